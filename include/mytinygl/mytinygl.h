@@ -1,0 +1,44 @@
+/*
+ * mytinygl.h — context API of the GB300 back end.
+ *
+ * The first four functions replace MyTinyGL's context API one for one
+ * (src/mytinygl.h:228-233): one current context per OS thread, created headless.
+ * The mtgl_* functions replace direct access to ctx->framebuffer
+ * (framebuffer_get_color_buffer, src/framebuffer.h:137, as used by
+ * include/mytinygl/sdl.h:76-80): the framebuffer lives in device memory, so reading
+ * it is an explicit, synchronising call.
+ */
+#ifndef MYTINYGL_GB300_CONTEXT_H
+#define MYTINYGL_GB300_CONTEXT_H
+
+#include <stdint.h>
+#include "GL/gl.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct GLState GLState;
+
+/* gl_create_context (gl_api.c:81): width/height in 1..16384; NULL on failure. */
+GLState *gl_create_context(int32_t width, int32_t height);
+void gl_destroy_context(GLState *ctx);
+void gl_make_current(GLState *ctx);
+GLState *gl_get_current_context(void);
+
+/* Wait for all queued rendering of ctx. Returns 0 or an mtgl_status code. */
+int mtgl_finish(GLState *ctx);
+/* Synchronise and return a host copy of the colour buffer (row 0 = top, packed
+ * a<<24|b<<16|g<<8|r). Valid until the next GL call on ctx. */
+const uint32_t *mtgl_color_buffer(GLState *ctx);
+/* Synchronise and copy whole buffers to caller memory; any pointer may be NULL. */
+int mtgl_read_framebuffer(GLState *ctx, uint32_t *color, float *depth, uint8_t *stencil);
+int mtgl_framebuffer_size(GLState *ctx, int32_t *width, int32_t *height);
+/* Name of the back end that renders this library's contexts. */
+const char *mtgl_backend_name(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MYTINYGL_GB300_CONTEXT_H */

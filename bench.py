@@ -1,0 +1,414 @@
+#!/usr/bin/env python3
+"""Headline benchmark: frames/s of the fixed-function pipeline on one GB300.
+
+Workload (default): the textured configuration — 1920x1080, 100k triangles whose clip-space
+vertices spill 1.5x past the frustum (~30 % clipped), per-vertex RGBA8 colour, uv in [0,4)
+with GL_REPEAT, a 512x512 RGBA8 noise texture sampled GL_LINEAR_MIPMAP_LINEAR and
+GL_MODULATE, 8 point lights with GL_COLOR_MATERIAL, GL_EXP fog (density 0.5), depth test
+GL_LESS. Seeded synthetic inputs (mytinygl_gb300/workloads.py), no dataset.
+
+A step is one frame: glClear, the frame's state calls and the glDrawArrays, submitted with
+glFlush. Lines printed (one JSON object each, rank 0 only):
+  value        frames/s with the vertex buffer and texture resident in device memory, timed
+               with CUDA events on the renderer's own stream; L2 is flushed (a 256 MiB write
+               on that stream) before every timed frame.
+  e2e          frames/s through the public C ABI with client vertex arrays: every step
+               copies the frame's vertex arrays host->device and reads the colour buffer
+               back (mtgl_read_framebuffer), timed on the host clock.
+  roofline     the tile raster/ROP kernel (K4): compulsory bytes per launch over its mean
+               launch time (CUDA events around the launch), against the measured HBM copy peak.
+  cpu_baseline the CPU oracle (a restatement of MyTinyGL's renderer) on all host cores, one
+               context per thread, on a bounded sample of the same frame.
+--impl reference times that CPU implementation as the measured arm.
+Several GPUs run independent replicas (one process per GPU, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+from mytinygl_gb300 import gl as G  # noqa: E402
+from mytinygl_gb300 import workloads as W  # noqa: E402
+
+WORKLOADS = {
+    "textured": dict(builder=W.textured_scene, full_tris=100_000, name="textured_clip_fog_1920x1080_100k",
+                     desc="1920x1080, 100k triangles (~30% clipped), 512^2 trilinear texture, 8 point lights, EXP fog"),
+    "rop": dict(builder=W.rop_scene, full_tris=1_000_000, name="rop_blend_stencil_1920x1080_1M",
+                desc="1920x1080, 1M small triangles, blend + alpha test + stencil INCR + depth LEQUAL, no depth writes"),
+    "sphere": dict(builder=W.sphere_scene, full_tris=1984, name="sphere_lit_800x600_1984",
+                   desc="800x600 UV sphere (1,984 triangles), directional light, GL_LESS, back-face culling"),
+}
+REC_BYTES = 192  # triangle record written by the setup kernel, read by the tile kernel
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in
+                ("draws", "input_triangles", "setup_triangles", "bin_entries", "fragments", "passes", "kernel_launches")]
+
+
+class Timings(ctypes.Structure):
+    _fields_ = [("vertex_ms", ctypes.c_double), ("setup_ms", ctypes.c_double), ("bin_ms", ctypes.c_double),
+                ("tile_ms", ctypes.c_double), ("passes", ctypes.c_uint64)]
+
+
+def bind_extras(lib):
+    L = lib.lib
+    L.mtgl_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+    L.mtgl_get_stats.restype = ctypes.c_int
+    L.mtgl_reset_stats.argtypes = [ctypes.c_void_p]
+    L.mtgl_reset_stats.restype = ctypes.c_int
+    L.mtgl_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.mtgl_set_profiling.restype = ctypes.c_int
+    L.mtgl_get_timings.argtypes = [ctypes.c_void_p, ctypes.POINTER(Timings)]
+    L.mtgl_get_timings.restype = ctypes.c_int
+    L.mtgl_cuda_stream.argtypes = [ctypes.c_void_p]
+    L.mtgl_cuda_stream.restype = ctypes.c_void_p
+
+
+def get_stats(ctx):
+    s = Stats()
+    assert ctx.glib.lib.mtgl_get_stats(ctx.handle, ctypes.byref(s)) == 0
+    return {k: int(getattr(s, k)) for k, _ in Stats._fields_}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(workload):
+    """DRAM bytes per K4 launch from the committed ncu summary, if one exists for the workload."""
+    path = os.path.join(REPO, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == workload and parts[1] == "k_tile":
+            return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def scene_bytes(scene, start):
+    """Bytes of client arrays the frame part passes by pointer (host->device per frame)."""
+    total = 0
+    for name, args in scene.cmds[start:]:
+        for a in args:
+            if isinstance(a, np.ndarray) and name.endswith("Pointer"):
+                total += a.nbytes
+    return total
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_ours(args, spec):
+    import torch
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import mytinygl_gb300 as M
+
+    M.build()
+    lib = M.library()
+    bind_extras(lib)
+
+    # ---- device-resident frames (value)
+    scene = spec["builder"](use_vbo=True)
+    fs = W.frame_start(scene)
+    ctx = lib.context(scene.width, scene.height)
+    scene.play(ctx, 0, fs)
+    for _ in range(args.warmup):
+        scene.play(ctx, fs)
+        ctx.glFinish()
+    stream_ptr = ctx.glib.lib.mtgl_cuda_stream(ctx.handle)
+    ext = torch.cuda.ExternalStream(stream_ptr)
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ctx.glib.lib.mtgl_reset_stats(ctx.handle)
+    ctx.glib.lib.mtgl_set_profiling(ctx.handle, 1)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ctx.glFinish()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            with torch.cuda.stream(ext):
+                flush_buf.zero_()
+                starts[i].record(ext)
+            scene.play(ctx, fs)
+            ctx.glFlush()
+            ends[i].record(ext)
+        ctx.glFinish()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    st = get_stats(ctx)
+    tm = Timings()
+    ctx.glib.lib.mtgl_get_timings(ctx.handle, ctypes.byref(tm))
+    ctx.glib.lib.mtgl_set_profiling(ctx.handle, 0)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    fps = world * args.steps / (total_ms / 1e3)
+    frags_per_frame = st["fragments"] / args.steps
+    ctx.destroy()
+
+    # ---- roofline of K4 (tile raster/ROP)
+    peak, peak_src = measured_peaks()
+    npix = scene.width * scene.height
+    tex_bytes = 0
+    for name, a in scene.cmds:
+        if name == "glTexImage2D":
+            w, h = int(a[3]), int(a[4])
+            tex_bytes += 4 * (w * h + (w // 2) * (h // 2))
+    rec = st["setup_triangles"] / args.steps
+    pairs = st["bin_entries"] / args.steps
+    k4_bytes = npix * 9 + pairs * 4 + rec * REC_BYTES + tex_bytes
+    k4_ms = tm.tile_ms / max(1, tm.passes)
+    achieved = k4_bytes / (k4_ms / 1e3) / 1e9 if k4_ms > 0 else None
+    traffic = ncu_traffic(spec["name"])
+
+    # ---- end to end through the C ABI with client arrays and readback (e2e)
+    escene = spec["builder"](use_vbo=False)
+    efs = W.frame_start(escene)
+    ectx = lib.context(escene.width, escene.height)
+    escene.play(ectx, 0, efs)
+    host = np.empty((escene.height, escene.width), np.uint32)
+    for _ in range(args.warmup):
+        escene.play(ectx, efs)
+        ectx.read(color=True, depth=False, stencil=False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        escene.play(ectx, efs)
+        ectx.glib.lib.mtgl_read_framebuffer(ectx.handle, host.ctypes.data, None, None)
+    e2e_s = time.perf_counter() - t0
+    ectx.destroy()
+    e2e_fps = world * args.steps / e2e_s
+    h2d = scene_bytes(escene, efs)
+    d2h = escene.width * escene.height * 4
+
+    out = {
+        "metric": "frames/s",
+        "value": round(fps, 3),
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded; mytinygl_gb300/workloads.py)",
+        "config": {"workload": spec["name"], "description": spec["desc"], "width": scene.width,
+                   "height": scene.height, "input_triangles": int(st["input_triangles"] / args.steps),
+                   "setup_triangles": int(rec), "bin_entries": int(pairs), "tile": 16,
+                   "l2": "flushed before every timed frame (256 MiB write on the renderer's stream)",
+                   "parallelism": f"replicas x{world}"},
+        "fragments_per_s": round(frags_per_frame * fps, 1),
+        "fragments_per_frame": int(frags_per_frame),
+        "triangles_per_s": round(st["input_triangles"] / args.steps * fps, 1),
+        "phase_ms": {"vertex": round(tm.vertex_ms / max(1, tm.passes), 4),
+                     "setup": round(tm.setup_ms / max(1, tm.passes), 4),
+                     "bin": round(tm.bin_ms / max(1, tm.passes), 4),
+                     "tile": round(k4_ms, 4)},
+        "wall_ms_per_step": round(wall * 1e3 / args.steps, 4),
+        "roofline": {"kernel": "k_tile (K4 tile raster/ROP)", "bound": "hbm",
+                     "achieved": round(achieved, 2) if achieved else None, "peak": peak,
+                     "peak_source": f"{peak_src} (HBM copy)", "unit": "GB/s",
+                     "frac": round(achieved / peak, 5) if achieved else None,
+                     "algorithmic_bytes_per_launch": int(k4_bytes),
+                     "traffic": traffic},
+        "e2e": {"value": round(e2e_fps, 3), "unit": "frames/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(st["kernel_launches"]),
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(spec, args.cpu_seconds)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def _oracle_lib():
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True, capture_output=True)
+    return G.load(os.path.join(REPO, "oracle", "_build", "libmtgl_oracle.so"))
+
+
+def cpu_frame_time(lib, spec, ntri, reps):
+    scene = spec["builder"](use_vbo=False, ntri=ntri) if spec["name"] != WORKLOADS["sphere"]["name"] else \
+        spec["builder"](use_vbo=False)
+    fs = W.frame_start(scene)
+    ctx = lib.context(scene.width, scene.height)
+    scene.play(ctx, 0, fs)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        scene.play(ctx, fs)
+    dt = time.perf_counter() - t0
+    ctx.destroy()
+    return dt / reps
+
+
+def cpu_baseline(spec, seconds):
+    """The oracle on every host core, one context per thread (the reference keeps one current
+    context per thread, gl_api.c:14-23), each rendering a sample of the frame's triangles."""
+    lib = _oracle_lib()
+    threads = os.cpu_count() or 1
+    full = spec["full_tris"]
+    sample = min(full, 500)
+    t1 = cpu_frame_time(lib, spec, sample, 1)
+    per_tri = t1 / sample
+    # about `seconds` of work per thread in total, at least one render each
+    sample = int(min(full, max(100, (seconds / 3.0) / max(per_tri, 1e-9))))
+    reps = 3 if sample < full else max(1, int(seconds / max(t1 * full / 500, 1e-6)))
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        times = list(ex.map(lambda _: cpu_frame_time(lib, spec, sample, reps), range(threads)))
+    wall = time.perf_counter() - t0
+    frame_s = statistics.median(times) * (full / sample)
+    return {"value": round(threads / frame_s, 5), "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": (f"first {sample} of {full} triangles of the same frame, {reps} renders per context, "
+                       f"{threads} contexts on {threads} threads; frame time scaled by {full}/{sample}"),
+            "wall_s": round(wall, 2)}
+
+
+def run_reference(args, spec):
+    world, rank, local = dist_init()
+    if rank != 0:
+        return None
+    lib = _oracle_lib()
+    threads = os.cpu_count() or 1
+    full = spec["full_tris"]
+    sample = min(full, 500)
+    t1 = cpu_frame_time(lib, spec, sample, 1)
+    budget = 120.0 / max(1, args.steps + args.warmup)  # whole run within a couple of minutes
+    sample = int(min(full, max(100, budget / max(t1 / sample, 1e-9))))
+    step = lambda: list(cf.ThreadPoolExecutor(threads).map(lambda _: cpu_frame_time(lib, spec, sample, 1),
+                                                           range(threads)))
+    for _ in range(args.warmup):
+        step()
+    per = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        per.append(statistics.median(step()))
+    wall = time.perf_counter() - t0
+    frame_s = statistics.median(per) * (full / sample)
+    fps = threads / frame_s
+    desc = (f"first {sample} of {full} triangles of the frame per context, {threads} contexts on {threads} "
+            f"threads per step; frame time scaled by {full}/{sample}")
+    return {"impl": "reference", "metric": "frames/s", "value": round(fps, 5), "unit": "frames/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(wall * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; mytinygl_gb300/workloads.py)",
+            "config": {"workload": spec["name"], "description": spec["desc"]},
+            "cpu_baseline": {"value": round(fps, 5), "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": round(fps, 5), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="textured")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline work per thread")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
+    spec = WORKLOADS[args.workload]
+    out = run_reference(args, spec) if args.impl == "reference" else run_ours(args, spec)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -149,6 +149,13 @@ typedef struct {
     uint64_t passes, kernel_launches;
 } mtgl_stats;
 
+/* Device time per pipeline phase, summed over the passes since profiling was enabled
+ * (CUDA events recorded on the context's stream around each phase). */
+typedef struct {
+    double vertex_ms, setup_ms, bin_ms, tile_ms;
+    uint64_t passes;
+} mtgl_timings;
+
 /* ---- lifetime ---- */
 int mtgl_dev_create(int32_t width, int32_t height, mtgl_dev **out);
 int mtgl_dev_destroy(mtgl_dev *d);
@@ -181,6 +188,11 @@ int mtgl_dev_finish(mtgl_dev *d);  /* submit and wait                           
 int mtgl_dev_read(mtgl_dev *d, uint32_t *color, float *depth, uint8_t *stencil);
 int mtgl_dev_stats(mtgl_dev *d, mtgl_stats *out);
 int mtgl_dev_reset_stats(mtgl_dev *d);
+/* Per-phase device timing (off by default); enabling resets the sums. */
+int mtgl_dev_profile(mtgl_dev *d, int enable);
+int mtgl_dev_timings(mtgl_dev *d, mtgl_timings *out);
+/* The cudaStream_t every operation of this context runs on (NULL for a CPU back end). */
+void *mtgl_dev_stream(mtgl_dev *d);
 
 #ifdef __cplusplus
 }

@@ -13,6 +13,7 @@
 
 #include <stdint.h>
 #include "GL/gl.h"
+#include "mytinygl/mtgl_dev.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -36,6 +37,14 @@ int mtgl_read_framebuffer(GLState *ctx, uint32_t *color, float *depth, uint8_t *
 int mtgl_framebuffer_size(GLState *ctx, int32_t *width, int32_t *height);
 /* Name of the back end that renders this library's contexts. */
 const char *mtgl_backend_name(void);
+/* Pipeline counters (draws, triangles, fragments, passes, kernel launches) of ctx. */
+int mtgl_get_stats(GLState *ctx, mtgl_stats *out);
+int mtgl_reset_stats(GLState *ctx);
+/* Per-phase device timing of ctx's passes (vertex / setup / bin / tile). */
+int mtgl_set_profiling(GLState *ctx, int enable);
+int mtgl_get_timings(GLState *ctx, mtgl_timings *out);
+/* cudaStream_t of ctx, for callers that order their own GPU work with the renderer's. */
+void *mtgl_cuda_stream(GLState *ctx);
 
 #ifdef __cplusplus
 }

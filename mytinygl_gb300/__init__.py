@@ -1,0 +1,25 @@
+"""mytinygl_gb300 — MyTinyGL's OpenGL 1.5 fixed-function pipeline on a GB300 (sm_103a).
+
+The product is libmytinygl_gb300.so (C ABI: include/GL/gl.h, include/mytinygl/*.h). This
+package builds it in-tree and offers a ctypes binding (`gl`), scene scripts (`scene`) and
+the seeded synthetic workloads (`workloads`) used by the benchmark and the tests.
+"""
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB_PATH
+
+
+def build(verbose=False, force=False) -> str:
+    return _build.build(verbose=verbose, force=force)
+
+
+def library():
+    """Load libmytinygl_gb300.so. There is no CPU fallback: a missing library is an error,
+    and creating a context without a visible CUDA device fails."""
+    from . import gl
+
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is not built; run mytinygl_gb300.build() (nvcc, sm_103a)")
+    return gl.load(LIB_PATH)

@@ -1,0 +1,97 @@
+// dev_kernels.h — host-side launchers of the sm_103a kernels (one translation unit each).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mtgl_device.cuh"
+
+namespace mtgl {
+
+struct GeomArgs {
+    const DevDraw *draws;
+    const uint32_t *draw_vslot_base;  // per draw, ascending
+    const uint32_t *draw_tri_base;    // per draw, ascending
+    int32_t ndraws;
+    const mtgl_vertex_state *vstates;
+    const DevRaster *rasters;
+    PostVertex *verts;
+    PostEye *eyes;                    // null when no draw of the pass lights per fragment
+    uint32_t total_slots;
+    uint32_t total_tris;
+    FrameDims dims;
+    uint32_t *tri_counts;             // count pass output
+    const uint32_t *tri_offsets;      // emit pass input (exclusive scan of tri_counts)
+    float *records;                   // emit pass output, kRecWords per record
+    float *eye_records;               // emit pass output, kEyeWords per record (may be null)
+    uint32_t records_cap;             // records the output buffers hold (writes beyond are dropped)
+};
+
+// K1: per-vertex stage (gl_api.c:263-348) for every vertex slot of the pass.
+int launch_vertex(const GeomArgs &a, cudaStream_t s);
+// K2: primitive assembly, clipping, perspective divide, culling and triangle setup
+// (raster.c:451-529, 729-1017, 1199-1231); count pass then emit pass.
+int launch_setup_count(const GeomArgs &a, cudaStream_t s);
+int launch_setup_emit(const GeomArgs &a, cudaStream_t s);
+
+// Every launcher returns the number of kernels it launched.
+
+// Device-wide exclusive scan of n uint32 values (in place allowed); writes the total to
+// *total_dev. temp must hold scan_temp_words(n) words.
+size_t scan_temp_words(uint32_t n);
+int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, uint32_t *total_dev, cudaStream_t s);
+
+struct BinArgs {
+    const float *records;
+    uint32_t nrec;
+    FrameDims dims;
+    uint32_t *rec_tiles;        // per record tile count, then its exclusive scan (in place)
+    uint32_t *keys, *vals;      // pair buffers (capacity >= pairs)
+    uint32_t *keys_alt, *vals_alt;
+    uint32_t *tile_count;       // per tile (ntiles + 1 entries)
+    uint32_t *tile_start;       // exclusive scan of tile_count
+    uint32_t *radix_hist;       // radix histograms
+    uint32_t *scan_temp;
+    uint32_t *total_dev;
+    uint32_t npairs;            // set by the host after the count scan
+    uint32_t pairs_cap;         // pair capacity of keys/vals (writes beyond are dropped)
+};
+
+int launch_bin_count(const BinArgs &a, cudaStream_t s);
+int launch_bin_expand(const BinArgs &a, cudaStream_t s);
+// Stable sort of (tile, record) pairs by tile; result in keys/vals. Returns nothing; uses
+// keys_alt/vals_alt as ping-pong storage.
+int launch_bin_sort(BinArgs &a, cudaStream_t s);
+size_t radix_hist_words(uint32_t npairs);
+
+struct TileArgs {
+    const float *records;
+    const float *eye_records;
+    const uint32_t *tile_vals;   // record indices sorted by tile, submission order within a tile
+    const uint32_t *tile_start;  // per tile
+    const uint32_t *tile_count;
+    const DevRaster *rasters;
+    uint32_t nrasters;
+    const ClearOp *clears;
+    int32_t nclears;
+    FrameDims dims;
+    uint32_t *color;
+    float *depth;
+    uint8_t *stencil;
+    unsigned long long *fragments;
+};
+
+// K4: one CTA per 16x16 tile: clears, then every triangle of the tile in order through the
+// full fragment pipeline (raster.c:532-724), then one write-back.
+int launch_tile(const TileArgs &a, cudaStream_t s);
+
+// glClear without draws (gl_api.c:409-457)
+void launch_clear(const ClearOp *ops_host, int nops, FrameDims dims, uint32_t *color, float *depth, uint8_t *stencil,
+                  cudaStream_t s);
+// mip level 1 (textures.c:311-354)
+void launch_mip1(const uint32_t *base, int32_t w, int32_t h, uint32_t *mip, cudaStream_t s);
+// glDrawPixels blit (gl_api.c:1287-1376)
+void launch_draw_pixels(const uint32_t *img, int32_t rx, int32_t ry, int32_t w, int32_t h, const DevRaster *raster,
+                        FrameDims dims, uint32_t *color, float *depth, cudaStream_t s);
+
+}  // namespace mtgl

@@ -1,0 +1,280 @@
+// k_bin.cu — K3 binning: triangle records -> per-tile lists in submission order.
+//
+// No counterpart in the reference, which scans every triangle's bounding box on one thread
+// (raster.c:532-724). Here each record is expanded into one (tile, record) pair per 16x16
+// tile its clamped bounding box touches; pairs are generated in submission order and a
+// stable LSD radix sort on the tile id (warp match-any ranking plus prefix sums) groups
+// them by tile while keeping that order inside every tile. The tile kernel then walks each
+// list front to back, so blending and stencil updates happen in GL order.
+#include "dev_kernels.h"
+
+namespace mtgl {
+
+// ------------------------------------------------------------------ scan
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 2048 values per block
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += n;
+    }
+    return v;
+}
+
+// exclusive block scan of one value per thread; returns the block total in *total
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total)
+{
+    __shared__ uint32_t warp_sums[kScanThreads / 32 + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = warp_incl_scan(v);
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
+        uint32_t wi = warp_incl_scan(w);
+        if (lane < kScanThreads / 32) warp_sums[lane] = wi - w;
+        if (lane == kScanThreads / 32 - 1) warp_sums[kScanThreads / 32] = wi;
+    }
+    __syncthreads();
+    uint32_t r = warp_sums[warp] + incl - v;
+    *total = warp_sums[kScanThreads / 32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_block(const uint32_t *in, uint32_t *out, uint32_t n,
+                                                            uint32_t *block_sums, uint32_t *total_dev)
+{
+    const uint32_t base = blockIdx.x * (uint32_t)kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        v[i] = (base + i < n) ? in[base + i] : 0u;
+        sum += v[i];
+    }
+    uint32_t total;
+    uint32_t run = block_excl_scan(sum, &total);
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++) {
+        if (base + i < n) out[base + i] = run;
+        run += v[i];
+    }
+    if (threadIdx.x == 0) {
+        if (block_sums) block_sums[blockIdx.x] = total;
+        if (total_dev) *total_dev = total;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t *out, uint32_t n, const uint32_t *block_offsets)
+{
+    const uint32_t add = block_offsets[blockIdx.x];
+    const uint32_t base = blockIdx.x * (uint32_t)kScanTile + threadIdx.x * kScanItems;
+#pragma unroll
+    for (int i = 0; i < kScanItems; i++)
+        if (base + i < n) out[base + i] += add;
+}
+
+size_t scan_temp_words(uint32_t n)
+{
+    size_t words = 0;
+    while (n > (uint32_t)kScanTile) {
+        n = (n + kScanTile - 1) / kScanTile;
+        words += ((size_t)n + 63) & ~(size_t)63;
+    }
+    return words + 64;
+}
+
+int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, uint32_t *total_dev, cudaStream_t s)
+{
+    if (n == 0) {
+        cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), s);
+        return 0;
+    }
+    const uint32_t nb = (n + kScanTile - 1) / kScanTile;
+    if (nb == 1) {
+        k_scan_block<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr, total_dev);
+        return 1;
+    }
+    k_scan_block<<<nb, kScanThreads, 0, s>>>(in, out, n, temp, nullptr);
+    uint32_t *next = temp + (((size_t)nb + 63) & ~(size_t)63);
+    int k = launch_scan(temp, temp, nb, next, total_dev, s);
+    k_scan_add<<<nb, kScanThreads, 0, s>>>(out, n, temp);
+    return k + 2;
+}
+
+// ------------------------------------------------------------------ record -> tiles
+
+// The setup kernel clamps every bbox to the framebuffer; the clamps here only keep tile
+// indices inside the tile grid whatever a record holds.
+__device__ __forceinline__ void rec_tile_box(const float *rec, const FrameDims &dims, int &tx0, int &ty0, int &tx1,
+                                             int &ty1)
+{
+    const float4 b1 = __ldg(reinterpret_cast<const float4 *>(rec) + 1);
+    const float4 b2 = __ldg(reinterpret_cast<const float4 *>(rec) + 2);
+    tx0 = min(max(__float_as_int(b1.z), 0), dims.width - 1) / kTile;
+    ty0 = min(max(__float_as_int(b1.w), 0), dims.height - 1) / kTile;
+    tx1 = max(min(__float_as_int(b2.x), dims.width - 1) / kTile, tx0);
+    ty1 = max(min(__float_as_int(b2.y), dims.height - 1) / kTile, ty0);
+}
+
+__global__ void __launch_bounds__(256) k_bin_count(BinArgs A)
+{
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= A.nrec) return;
+    int tx0, ty0, tx1, ty1;
+    rec_tile_box(A.records + (size_t)r * kRecWords, A.dims, tx0, ty0, tx1, ty1);
+    A.rec_tiles[r] = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+}
+
+// one warp per record: lanes write the record's tiles row-major (pairs stay in submission order)
+__global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
+{
+    const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= A.nrec) return;
+    int tx0, ty0, tx1, ty1;
+    rec_tile_box(A.records + (size_t)r * kRecWords, A.dims, tx0, ty0, tx1, ty1);
+    const int w = tx1 - tx0 + 1;
+    const int cnt = w * (ty1 - ty0 + 1);
+    const uint32_t base = A.rec_tiles[r];
+    for (int i = lane; i < cnt; i += 32) {
+        if (base + (uint32_t)i >= A.pairs_cap) break;
+        const int tx = tx0 + i % w, ty = ty0 + i / w;
+        const uint32_t tile = (uint32_t)(ty * A.dims.tiles_x + tx);
+        A.keys[base + i] = tile;
+        A.vals[base + i] = r;
+        atomicAdd(A.tile_count + tile, 1u);
+    }
+}
+
+int launch_bin_count(const BinArgs &a, cudaStream_t s)
+{
+    if (!a.nrec) return 0;
+    k_bin_count<<<(a.nrec + 255) / 256, 256, 0, s>>>(a);
+    return 1;
+}
+
+int launch_bin_expand(const BinArgs &a, cudaStream_t s)
+{
+    if (!a.nrec) return 0;
+    const uint64_t threads = (uint64_t)a.nrec * 32;
+    k_bin_expand<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a);
+    return 1;
+}
+
+// ------------------------------------------------------------------ stable radix sort by tile
+
+constexpr int kRadixThreads = 256;
+constexpr int kRadixWarps = kRadixThreads / 32;
+constexpr int kRadixItems = 8;  // per thread
+constexpr int kRadixTile = kRadixThreads * kRadixItems;
+constexpr int kRadixDigits = 256;
+
+size_t radix_hist_words(uint32_t npairs)
+{
+    const size_t nb = (npairs + kRadixTile - 1) / kRadixTile;
+    return nb * kRadixDigits + 64;
+}
+
+__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t *keys, uint32_t n, int shift,
+                                                             uint32_t mask, uint32_t *hist, uint32_t nblocks)
+{
+    __shared__ uint32_t h[kRadixDigits];
+    for (int i = threadIdx.x; i < kRadixDigits; i += kRadixThreads) h[i] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * (uint32_t)kRadixTile;
+#pragma unroll
+    for (int k = 0; k < kRadixItems; k++) {
+        const uint32_t i = base + k * kRadixThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & mask], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadixDigits; d += kRadixThreads) hist[(size_t)d * nblocks + blockIdx.x] = h[d];
+}
+
+// Stable scatter: warp w owns items [w*256, w*256+256) of the block, taken 32 at a time in
+// order; match-any groups equal digits, the leader advances the warp's digit counter, and
+// per-digit prefix sums over warps and blocks place every item after all earlier ones.
+__global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t *keys, const uint32_t *vals,
+                                                                uint32_t n, int shift, uint32_t mask,
+                                                                const uint32_t *hist_scan, uint32_t nblocks,
+                                                                uint32_t *keys_out, uint32_t *vals_out)
+{
+    __shared__ uint32_t wcount[kRadixWarps][kRadixDigits];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kRadixWarps * kRadixDigits; i += kRadixThreads) (&wcount[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t wbase = blockIdx.x * (uint32_t)kRadixTile + warp * 32 * kRadixItems;
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t key[kRadixItems], val[kRadixItems], rank[kRadixItems];
+#pragma unroll
+    for (int k = 0; k < kRadixItems; k++) {
+        const uint32_t i = wbase + k * 32 + lane;
+        const bool valid = i < n;
+        key[k] = valid ? keys[i] : 0u;
+        val[k] = valid ? vals[i] : 0u;
+        const uint32_t d = valid ? ((key[k] >> shift) & mask) : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        const uint32_t pre = valid ? wcount[warp][d] : 0u;
+        __syncwarp();
+        if (valid && lane == leader) wcount[warp][d] = pre + __popc(peers);
+        __syncwarp();
+        rank[k] = pre + __popc(peers & lt);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadixDigits; d += kRadixThreads) {
+        uint32_t run = hist_scan[(size_t)d * nblocks + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < kRadixWarps; w++) {
+            const uint32_t c = wcount[w][d];
+            wcount[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kRadixItems; k++) {
+        const uint32_t i = wbase + k * 32 + lane;
+        if (i < n) {
+            const uint32_t d = (key[k] >> shift) & mask;
+            const uint32_t pos = wcount[warp][d] + rank[k];
+            keys_out[pos] = key[k];
+            vals_out[pos] = val[k];
+        }
+    }
+}
+
+int launch_bin_sort(BinArgs &a, cudaStream_t s)
+{
+    const uint32_t n = a.npairs;
+    if (n <= 1) return 0;
+    int launches = 0;
+    const uint32_t ntiles = (uint32_t)(a.dims.tiles_x * a.dims.tiles_y);
+    int bits = 1;
+    while (bits < 32 && (1u << bits) < ntiles) bits++;
+    const uint32_t nb = (n + kRadixTile - 1) / kRadixTile;
+    for (int shift = 0; shift < bits; shift += 8) {
+        const int nbits = (bits - shift) < 8 ? (bits - shift) : 8;
+        const uint32_t mask = (1u << nbits) - 1u;
+        k_radix_hist<<<nb, kRadixThreads, 0, s>>>(a.keys, n, shift, mask, a.radix_hist, nb);
+        launches += 2 + launch_scan(a.radix_hist, a.radix_hist, nb * kRadixDigits, a.scan_temp, a.total_dev, s);
+        k_radix_scatter<<<nb, kRadixThreads, 0, s>>>(a.keys, a.vals, n, shift, mask, a.radix_hist, nb, a.keys_alt,
+                                                     a.vals_alt);
+        uint32_t *tk = a.keys, *tv = a.vals;
+        a.keys = a.keys_alt;
+        a.vals = a.vals_alt;
+        a.keys_alt = tk;
+        a.vals_alt = tv;
+    }
+    return launches;
+}
+
+}  // namespace mtgl

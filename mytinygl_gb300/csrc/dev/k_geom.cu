@@ -1,0 +1,503 @@
+// k_geom.cu — K1 vertex stage and K2 assembly / clip / cull / triangle setup.
+//
+// K1 runs emit_vertex (gl_api.c:263-348) for every vertex slot of the pass: one thread per
+// slot, attribute fetch with the conversions of get_array_element and glColor4f
+// (gl_api.c:694-723, 1758-1797). K2 runs once per input triangle in submission order:
+// primitive assembly (raster.c:961-1017, 1199-1231), Sutherland-Hodgman clipping against
+// N,F,L,R,B,T (clipping.h:37-126), perspective divide (raster.c:729-746), the fan loop with
+// culling (raster.c:751-774, 901-958) and the per-triangle part of
+// rasterize_triangle_smooth (raster.c:458-529). The count pass sizes the output; after an
+// exclusive scan the emit pass writes each record at its submission-order position.
+#include "dev_kernels.h"
+
+namespace mtgl {
+
+__device__ __forceinline__ int find_base(const uint32_t *base, int n, uint32_t g)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(base + mid) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ float ld_f32(const uint8_t *p)
+{
+    if ((reinterpret_cast<uintptr_t>(p) & 3u) == 0) return __ldg(reinterpret_cast<const float *>(p));
+    uint32_t v = (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8) | ((uint32_t)__ldg(p + 2) << 16) |
+                 ((uint32_t)__ldg(p + 3) << 24);
+    return __uint_as_float(v);
+}
+
+__device__ __forceinline__ uint32_t read_index(const uint8_t *idx, uint32_t type, uint32_t k)
+{
+    if (type == GL_UNSIGNED_INT) {
+        const uint8_t *p = idx + 4ull * k;
+        if ((reinterpret_cast<uintptr_t>(p) & 3u) == 0) return __ldg(reinterpret_cast<const uint32_t *>(p));
+        return (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8) | ((uint32_t)__ldg(p + 2) << 16) |
+               ((uint32_t)__ldg(p + 3) << 24);
+    }
+    if (type == GL_UNSIGNED_SHORT) {
+        const uint8_t *p = idx + 2ull * k;
+        return (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8);
+    }
+    return __ldg(idx + k);
+}
+
+// get_array_element (gl_api.c:1758-1797); reads past a buffer's end give zeros (the
+// reference reads whatever memory follows, which is undefined).
+template <int N>
+__device__ __forceinline__ void fetch_attr(const DevAttrib &a, int64_t index, float *out)
+{
+    if (index < 0) {
+#pragma unroll
+        for (int i = 0; i < N; i++) out[i] = (i < 3) ? 0.0f : 1.0f;
+        return;
+    }
+    const int comp = a.type == GL_FLOAT ? 4 : 1;
+    const int64_t rel = index - a.base_index;
+    const uint64_t need = (uint64_t)a.size * (uint64_t)comp;
+    if (!a.ptr || rel < 0 || a.stride <= 0 || (uint64_t)rel * (uint64_t)a.stride + need > a.bytes) {
+#pragma unroll
+        for (int i = 0; i < N; i++) out[i] = (i == 3) ? 1.0f : 0.0f;
+        return;
+    }
+    const uint8_t *p = a.ptr + (uint64_t)rel * (uint64_t)a.stride;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        if (i < a.size) out[i] = (a.type == GL_FLOAT) ? ld_f32(p + 4 * i) : u8f(__ldg(p + i));
+        else out[i] = (i == 3) ? 1.0f : 0.0f;
+    }
+}
+
+// glColor4f's sanitising (gl_api.c:711-723)
+__device__ __forceinline__ float sanitize(float v, bool alpha)
+{
+    if (isnan(v) || isinf(v)) v = alpha ? 1.0f : 0.0f;
+    return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+}
+
+__global__ void __launch_bounds__(128) k_vertex(GeomArgs A)
+{
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= A.total_slots) return;
+    const int d = find_base(A.draw_vslot_base, A.ndraws, g);
+    const DevDraw &D = A.draws[d];
+    const uint32_t k = g - D.vslot_base;
+    int64_t src;
+    uint32_t vsi = D.vs_base;
+    if (D.range_mode) {
+        src = ((int64_t)k < (int64_t)D.range_n) ? D.index_min + (int64_t)k : -1;
+    } else {
+        src = D.index_type ? (int64_t)(int32_t)read_index(D.indices, D.index_type, k) : (int64_t)D.first + k;
+        if (D.vs_ids) vsi += __ldg(D.vs_ids + k);
+    }
+    const mtgl_vertex_state &V = A.vstates[vsi];
+
+    float p[4], c[4], t[2], n[3];
+    fetch_attr<4>(D.pos, src, p);
+    const float x = p[0], y = p[1], z = D.pos2d ? 0.0f : p[2];
+    if (D.color.enabled) {
+        fetch_attr<4>(D.color, src, c);
+#pragma unroll
+        for (int i = 0; i < 4; i++) c[i] = sanitize(c[i], i == 3);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; i++) c[i] = D.cur_color[i];
+    }
+    if (D.tex.enabled) fetch_attr<2>(D.tex, src, t);
+    else { t[0] = D.cur_tex[0]; t[1] = D.cur_tex[1]; }
+    if (D.normal.enabled) fetch_attr<3>(D.normal, src, n);
+    else { n[0] = D.cur_normal[0]; n[1] = D.cur_normal[1]; n[2] = D.cur_normal[2]; }
+
+    const float4 eye = mul_m4(V.modelview, x, y, z, 1.0f);
+    const float4 n4 = mul_m4(V.normal_matrix, n[0], n[1], n[2], 0.0f);
+    const float3 en = normalize3(n4.x, n4.y, n4.z);
+    const float3 ep = make_float3(eye.x, eye.y, eye.z);
+    float4 vc = make_float4(c[0], c[1], c[2], c[3]);
+    if (V.lighting && !V.phong) {
+        mtgl_material front = V.lit.front;
+        if (V.color_material &&
+            (V.color_material_face == GL_FRONT || V.color_material_face == GL_FRONT_AND_BACK)) {
+            // GL_COLOR_MATERIAL: the clamped vertex colour replaces material fields (gl_api.c:285-312)
+            const float cc[4] = {clamp01(c[0]), clamp01(c[1]), clamp01(c[2]), clamp01(c[3])};
+            const uint32_t mode = V.color_material_mode;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                if (mode == GL_AMBIENT || mode == GL_AMBIENT_AND_DIFFUSE) front.ambient[i] = cc[i];
+                if (mode == GL_DIFFUSE || mode == GL_AMBIENT_AND_DIFFUSE) front.diffuse[i] = cc[i];
+                if (mode == GL_SPECULAR) front.specular[i] = cc[i];
+                if (mode == GL_EMISSION) front.emission[i] = cc[i];
+            }
+        }
+        vc = compute_lighting(V.lit, ep, en, front);
+    }
+    const float4 clip = mul_m4(V.projection, eye.x, eye.y, eye.z, eye.w);
+    const float4 t4 = mul_m4(V.texture, t[0], t[1], 0.0f, 1.0f);
+    float2 uv;
+    if (t4.w != 0.0f && t4.w != 1.0f) uv = make_float2(t4.x / t4.w, t4.y / t4.w);
+    else uv = make_float2(t4.x, t4.y);
+
+    PostVertex o;
+    o.clip = clip;
+    o.color = vc;
+    o.uv = uv;
+    o.eye_z = -eye.z;
+    o.pad = 0.0f;
+    A.verts[g] = o;
+    if (A.eyes) {
+        PostEye e;
+        e.pos_nx = make_float4(ep.x, ep.y, ep.z, en.x);
+        e.nyz = make_float4(en.y, en.z, 0.0f, 0.0f);
+        A.eyes[g] = e;
+    }
+}
+
+// ------------------------------------------------------------------ K2
+
+struct CV {
+    float4 clip;
+    float4 col;
+    float2 uv;
+    float ez;
+    float3 ep, en;
+};
+
+// vertex_lerp (graphics.h:465-475): colour uses a*(1-t)+b*t, the rest a+t*(b-a)
+__device__ __forceinline__ CV cv_lerp(const CV &a, const CV &b, float t)
+{
+    CV v;
+    v.clip = make_float4(a.clip.x + t * (b.clip.x - a.clip.x), a.clip.y + t * (b.clip.y - a.clip.y),
+                         a.clip.z + t * (b.clip.z - a.clip.z), a.clip.w + t * (b.clip.w - a.clip.w));
+    v.col = lerp_col(a.col, b.col, t);
+    v.uv = make_float2(a.uv.x + t * (b.uv.x - a.uv.x), a.uv.y + t * (b.uv.y - a.uv.y));
+    v.ez = a.ez + t * (b.ez - a.ez);
+    v.ep = make_float3(a.ep.x + t * (b.ep.x - a.ep.x), a.ep.y + t * (b.ep.y - a.ep.y), a.ep.z + t * (b.ep.z - a.ep.z));
+    v.en = make_float3(a.en.x + t * (b.en.x - a.en.x), a.en.y + t * (b.en.y - a.en.y), a.en.z + t * (b.en.z - a.en.z));
+    return v;
+}
+
+__device__ __forceinline__ float plane_dist(const float4 &v, int p)
+{
+    switch (p) {
+    case 0: return v.z + v.w;   // near
+    case 1: return v.w - v.z;   // far
+    case 2: return v.x + v.w;   // left
+    case 3: return v.w - v.x;   // right
+    case 4: return v.y + v.w;   // bottom
+    default: return v.w - v.y;  // top
+    }
+}
+
+__device__ __forceinline__ void snap_plane(CV &v, int p)
+{
+    switch (p) {
+    case 2: v.clip.x = -v.clip.w; break;
+    case 3: v.clip.x = v.clip.w; break;
+    case 4: v.clip.y = -v.clip.w; break;
+    case 5: v.clip.y = v.clip.w; break;
+    case 0: v.clip.z = -v.clip.w; break;
+    default: v.clip.z = v.clip.w; break;
+    }
+}
+
+// MAX_CLIP_VERTS (clipping.h:16). A planar triangle gains at most one vertex per plane, so
+// nine suffice; only non-finite inputs, undefined in the reference, could ask for more, and
+// those extra vertices are dropped instead of written out of bounds.
+constexpr int kClipMax = 12;
+
+// clip_triangle (clipping.h:106-126): six Sutherland-Hodgman passes; result in bufA[0..n)
+__device__ __noinline__ int clip_triangle(CV *bufA, CV *bufB)
+{
+    int n = 3;
+    CV *in = bufA, *out = bufB;
+    for (int p = 0; p < 6; p++) {
+        int m = 0;
+        const CV *prev = &in[n - 1];
+        float pd = plane_dist(prev->clip, p);
+        for (int i = 0; i < n; i++) {
+            const CV *cur = &in[i];
+            float cd = plane_dist(cur->clip, p);
+            if (pd >= 0) {
+                if (cd >= 0) {
+                    if (m < kClipMax) out[m++] = *cur;
+                } else {
+                    float den = pd - cd;
+                    if (fabsf(den) > 1e-10f && m < kClipMax) {
+                        out[m] = cv_lerp(*prev, *cur, pd / den);
+                        snap_plane(out[m], p);
+                        m++;
+                    }
+                }
+            } else if (cd >= 0) {
+                float den = pd - cd;
+                if (fabsf(den) > 1e-10f && m < kClipMax) {
+                    out[m] = cv_lerp(*prev, *cur, pd / den);
+                    snap_plane(out[m], p);
+                    m++;
+                }
+                if (m < kClipMax) out[m++] = *cur;
+            }
+            prev = cur;
+            pd = cd;
+        }
+        n = m;
+        CV *tmp = in;
+        in = out;
+        out = tmp;
+        if (n == 0) return 0;
+    }
+    // after six passes the result is in `in`; move it to bufA if needed
+    if (in != bufA)
+        for (int i = 0; i < n; i++) bufA[i] = in[i];
+    return n;
+}
+
+__device__ __forceinline__ void persp_divide(CV &v)
+{
+    if (fabsf(v.clip.w) < 1e-6f) {
+        v.clip = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        return;
+    }
+    float iw = 1.0f / v.clip.w;
+    v.clip.x *= iw;
+    v.clip.y *= iw;
+    v.clip.z *= iw;
+    v.clip.w = iw;
+}
+
+__device__ __forceinline__ void ndc_to_screen(const mtgl_raster_state &rs, float x, float y, int32_t &sx, int32_t &sy)
+{
+    sx = x86_f2i((x + 1.0f) * 0.5f * (float)rs.viewport[2] + (float)rs.viewport[0]);
+    sy = x86_f2i((1.0f - y) * 0.5f * (float)rs.viewport[3] + (float)rs.viewport[1]);
+}
+
+__device__ __forceinline__ float idiff(int32_t a, int32_t b) { return (float)(int32_t)((uint32_t)a - (uint32_t)b); }
+
+__device__ __forceinline__ bool culled(const mtgl_raster_state &rs, float sa)
+{
+    if (!rs.cull_face) return false;
+    bool front = (rs.front_face == GL_CCW) ? (sa < 0) : (sa > 0);
+    if (rs.cull_face_mode == GL_FRONT) return front;
+    if (rs.cull_face_mode == GL_BACK) return !front;
+    return true;
+}
+
+__device__ __forceinline__ void element_triple(uint32_t mode, uint32_t k, uint32_t &a, uint32_t &b, uint32_t &c)
+{
+    switch (mode) {
+    case GL_TRIANGLE_STRIP:
+        if (k % 2 == 0) { a = k; b = k + 1; c = k + 2; }
+        else { a = k + 1; b = k; c = k + 2; }
+        break;
+    case GL_TRIANGLE_FAN:
+    case GL_POLYGON:
+        a = 0; b = k + 1; c = k + 2;
+        break;
+    case GL_QUADS: {
+        uint32_t q = 4 * (k / 2);
+        if (k % 2 == 0) { a = q; b = q + 1; c = q + 2; }
+        else { a = q; b = q + 2; c = q + 3; }
+        break;
+    }
+    case GL_QUAD_STRIP: {
+        uint32_t i = 2 * (k / 2);
+        if (k % 2 == 0) { a = i; b = i + 1; c = i + 3; }
+        else { a = i; b = i + 3; c = i + 2; }
+        break;
+    }
+    default:
+        a = 3 * k; b = 3 * k + 1; c = 3 * k + 2;
+        break;
+    }
+}
+
+__device__ __forceinline__ uint32_t element_slot(const DevDraw &D, uint32_t e)
+{
+    if (!D.range_mode) return D.vslot_base + e;
+    const int32_t idx = (int32_t)read_index(D.indices, D.index_type, e);
+    const int64_t rel = (int64_t)idx - D.index_min;
+    // negative indices read the default attributes (gl_api.c:1766); the range check only
+    // guards against an index range that does not describe the indices
+    if (idx < 0 || rel < 0 || rel >= (int64_t)D.range_n) return D.vslot_base + (uint32_t)D.range_n;
+    return D.vslot_base + (uint32_t)rel;
+}
+
+__device__ __forceinline__ void load_cv(const GeomArgs &A, uint32_t slot, bool eye, CV &v)
+{
+    const PostVertex pv = A.verts[slot];
+    v.clip = pv.clip;
+    v.col = pv.color;
+    v.uv = pv.uv;
+    v.ez = pv.eye_z;
+    if (eye) {
+        const PostEye e = A.eyes[slot];
+        v.ep = make_float3(e.pos_nx.x, e.pos_nx.y, e.pos_nx.z);
+        v.en = make_float3(e.pos_nx.w, e.nyz.x, e.nyz.y);
+    } else {
+        v.ep = make_float3(0.0f, 0.0f, 0.0f);
+        v.en = make_float3(0.0f, 0.0f, 1.0f);
+    }
+}
+
+// Per fan triangle: the setup half of rasterize_triangle_smooth. Returns true when the
+// triangle produces a record; writes it when `rec` is non-null.
+__device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raster_id, const FrameDims &dims, const CV &a,
+                                              const CV &b, const CV &c, float *rec, float *eyerec)
+{
+    const mtgl_raster_state &rs = R.rs;
+    int32_t x0, y0, x1, y1, x2, y2;
+    ndc_to_screen(rs, a.clip.x, a.clip.y, x0, y0);
+    ndc_to_screen(rs, b.clip.x, b.clip.y, x1, y1);
+    ndc_to_screen(rs, c.clip.x, c.clip.y, x2, y2);
+    const float sa = idiff(x1, x0) * idiff(y2, y0) - idiff(x2, x0) * idiff(y1, y0);
+    if (culled(rs, sa)) return false;
+    const bool back = (rs.front_face == GL_CCW) ? (sa >= 0) : (sa < 0);
+
+    int32_t minX = x0 < x1 ? (x0 < x2 ? x0 : x2) : (x1 < x2 ? x1 : x2);
+    int32_t minY = y0 < y1 ? (y0 < y2 ? y0 : y2) : (y1 < y2 ? y1 : y2);
+    int32_t maxX = x0 > x1 ? (x0 > x2 ? x0 : x2) : (x1 > x2 ? x1 : x2);
+    int32_t maxY = y0 > y1 ? (y0 > y2 ? y0 : y2) : (y1 > y2 ? y1 : y2);
+    if (minX < rs.viewport[0]) minX = rs.viewport[0];
+    if (minY < rs.viewport[1]) minY = rs.viewport[1];
+    if (maxX >= rs.viewport[0] + rs.viewport[2]) maxX = rs.viewport[0] + rs.viewport[2] - 1;
+    if (maxY >= rs.viewport[1] + rs.viewport[3]) maxY = rs.viewport[1] + rs.viewport[3] - 1;
+    if (rs.scissor_test) {
+        if (minX < rs.scissor[0]) minX = rs.scissor[0];
+        if (minY < rs.scissor[1]) minY = rs.scissor[1];
+        if (maxX >= rs.scissor[0] + rs.scissor[2]) maxX = rs.scissor[0] + rs.scissor[2] - 1;
+        if (maxY >= rs.scissor[1] + rs.scissor[3]) maxY = rs.scissor[1] + rs.scissor[3] - 1;
+    }
+    if (minX > maxX || minY > maxY) return false;
+    // pixels outside the framebuffer read defaults and write nothing (framebuffer.h:92-134)
+    if (minX < 0) minX = 0;
+    if (minY < 0) minY = 0;
+    if (maxX > dims.width - 1) maxX = dims.width - 1;
+    if (maxY > dims.height - 1) maxY = dims.height - 1;
+    if (minX > maxX || minY > maxY) return false;
+
+    const float fx0 = (float)x0, fy0 = (float)y0, fx1 = (float)x1, fy1 = (float)y1, fx2 = (float)x2, fy2 = (float)y2;
+    const float area = (fx2 - fx0) * (fy1 - fy0) - (fy2 - fy0) * (fx1 - fx0);
+    if (fabsf(area) < 0.5f) return false;
+    if (!rec) return true;
+
+    const float inv_area = 1.0f / area;
+    float lod = 0.0f;
+    if (R.tex) {
+        const float screen_area = fabsf(area) * 0.5f;
+        const float du1 = (b.uv.x - a.uv.x) * (float)R.tex_w;
+        const float dv1 = (b.uv.y - a.uv.y) * (float)R.tex_h;
+        const float du2 = (c.uv.x - a.uv.x) * (float)R.tex_w;
+        const float dv2 = (c.uv.y - a.uv.y) * (float)R.tex_h;
+        const float texel_area = fabsf(du1 * dv2 - du2 * dv1) * 0.5f;
+        if (screen_area > 0.0f) {
+            const float tpp = texel_area / screen_area;
+            if (tpp > 0.0f) {
+                lod = log2f(tpp) * 0.5f;
+                if (lod < 0.0f) lod = 0.0f;
+            }
+        }
+    }
+    float4 *r4 = reinterpret_cast<float4 *>(rec);
+    r4[0] = make_float4(fx0, fy0, fx1, fy1);
+    r4[1] = make_float4(fx2, fy2, __int_as_float(minX), __int_as_float(minY));
+    r4[2] = make_float4(__int_as_float(maxX), __int_as_float(maxY), area, inv_area);
+    r4[3] = make_float4(a.clip.z, b.clip.z, c.clip.z, a.clip.w);
+    r4[4] = make_float4(b.clip.w, c.clip.w, a.col.x, a.col.y);
+    r4[5] = make_float4(a.col.z, a.col.w, b.col.x, b.col.y);
+    r4[6] = make_float4(b.col.z, b.col.w, c.col.x, c.col.y);
+    r4[7] = make_float4(c.col.z, c.col.w, a.uv.x, a.uv.y);
+    r4[8] = make_float4(b.uv.x, b.uv.y, c.uv.x, c.uv.y);
+    r4[9] = make_float4(a.uv.x * a.clip.w, a.uv.y * a.clip.w, b.uv.x * b.clip.w, b.uv.y * b.clip.w);
+    r4[10] = make_float4(c.uv.x * c.clip.w, c.uv.y * c.clip.w, a.ez, b.ez);
+    r4[11] = make_float4(c.ez, lod, __uint_as_float(raster_id), __uint_as_float(back ? 1u : 0u));
+    if (eyerec) {
+        float4 *e4 = reinterpret_cast<float4 *>(eyerec);
+        e4[0] = make_float4(a.ep.x, a.ep.y, a.ep.z, a.en.x);
+        e4[1] = make_float4(a.en.y, a.en.z, b.ep.x, b.ep.y);
+        e4[2] = make_float4(b.ep.z, b.en.x, b.en.y, b.en.z);
+        e4[3] = make_float4(c.ep.x, c.ep.y, c.ep.z, c.en.x);
+        e4[4] = make_float4(c.en.y, c.en.z, 0.0f, 0.0f);
+    }
+    return true;
+}
+
+template <bool EMIT>
+__global__ void __launch_bounds__(128) k_setup(GeomArgs A)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.total_tris) return;
+    const int d = find_base(A.draw_tri_base, A.ndraws, t);
+    const DevDraw &D = A.draws[d];
+    const uint32_t k = t - D.tri_base;
+    uint32_t e0, e1, e2;
+    element_triple(D.mode, k, e0, e1, e2);
+    const DevRaster &R = A.rasters[D.raster];
+    const bool eye = R.needs_eye && A.eyes;
+
+    CV v0, v1, v2;
+    load_cv(A, element_slot(D, e0), eye, v0);
+    load_cv(A, element_slot(D, e1), eye, v1);
+    load_cv(A, element_slot(D, e2), eye, v2);
+
+    // all three vertices inside all six planes: the clipper returns the triangle unchanged
+    bool inside = true;
+#pragma unroll
+    for (int p = 0; p < 6; p++)
+        inside = inside && (plane_dist(v0.clip, p) >= 0.0f) && (plane_dist(v1.clip, p) >= 0.0f) &&
+                 (plane_dist(v2.clip, p) >= 0.0f);
+    const uint32_t out = EMIT ? A.tri_offsets[t] : 0;
+    const bool write_eye = EMIT && eye && A.eye_records;
+    uint32_t produced = 0;
+    if (inside) {
+        persp_divide(v0);
+        persp_divide(v1);
+        persp_divide(v2);
+        const bool room = out < A.records_cap;
+        float *rec = (EMIT && room) ? A.records + (size_t)out * kRecWords : nullptr;
+        float *erec = (write_eye && room) ? A.eye_records + (size_t)out * kEyeWords : nullptr;
+        if ((EMIT && !room) || setup_fan_tri(R, D.raster, A.dims, v0, v1, v2, rec, erec)) produced = 1;
+    } else {
+        CV bufA[kClipMax], bufB[kClipMax];
+        bufA[0] = v0;
+        bufA[1] = v1;
+        bufA[2] = v2;
+        const int n = clip_triangle(bufA, bufB);
+        if (n >= 3) {
+            for (int j = 0; j < n; j++) persp_divide(bufA[j]);
+            for (int j = 1; j + 1 < n; j++) {
+                const bool room = out + produced < A.records_cap;
+                if (EMIT && !room) break;
+                float *rec = EMIT ? A.records + (size_t)(out + produced) * kRecWords : nullptr;
+                float *erec = write_eye ? A.eye_records + (size_t)(out + produced) * kEyeWords : nullptr;
+                if (setup_fan_tri(R, D.raster, A.dims, bufA[0], bufA[j], bufA[j + 1], rec, erec)) produced++;
+            }
+        }
+    }
+    if (!EMIT) A.tri_counts[t] = produced;
+}
+
+int launch_vertex(const GeomArgs &a, cudaStream_t s)
+{
+    if (!a.total_slots) return 0;
+    k_vertex<<<(a.total_slots + 127) / 128, 128, 0, s>>>(a);
+    return 1;
+}
+
+int launch_setup_count(const GeomArgs &a, cudaStream_t s)
+{
+    if (!a.total_tris) return 0;
+    k_setup<false><<<(a.total_tris + 127) / 128, 128, 0, s>>>(a);
+    return 1;
+}
+
+int launch_setup_emit(const GeomArgs &a, cudaStream_t s)
+{
+    if (!a.total_tris) return 0;
+    k_setup<true><<<(a.total_tris + 127) / 128, 128, 0, s>>>(a);
+    return 1;
+}
+
+}  // namespace mtgl

@@ -1,0 +1,211 @@
+// k_tile.cu — K4 tile raster/ROP (replaces rasterize_triangle_smooth's pixel loop,
+// raster.c:532-724, and glClear's loops, gl_api.c:409-457).
+//
+// One CTA owns one 16x16 tile; thread t owns one pixel for the whole pass, so the pixel's
+// colour, depth and stencil stay in registers between triangles. Each warp covers an 8x4
+// block of the tile. The CTA walks the tile's record list (submission order, built by the
+// binning pass) in chunks staged through shared memory; every thread runs the reference's
+// fragment pipeline for its own pixel: edge functions at the integer pixel position,
+// barycentrics, stencil test/ops, depth test, colour (flat / smooth / per-fragment
+// lighting), texture with alpha test and texenv, fog, depth write, blend, masked write.
+// Because a pixel is only ever touched by its own thread, in-order blending and stencil
+// updates need no atomics. Clears of the pass are applied first; a clear that covers the
+// whole tile means that buffer is never read from memory.
+#include "dev_kernels.h"
+
+namespace mtgl {
+
+constexpr int kChunk = 32;  // records staged per step
+
+__device__ __forceinline__ bool covers_tile(const ClearOp &c, uint32_t bit, int x0, int y0, int x1, int y1)
+{
+    return (c.mask & bit) && c.x0 <= x0 && c.y0 <= y0 && c.x1 >= x1 && c.y1 >= y1;
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
+{
+    __shared__ float4 s_rec[kChunk][kRecWords / 4];
+    __shared__ float4 s_eye[kChunk][kEyeWords / 4];
+
+    const int tile = blockIdx.x;
+    const int tx = tile % A.dims.tiles_x, ty = tile / A.dims.tiles_x;
+    const uint32_t count = A.tile_count[tile];
+    if (count == 0 && A.nclears == 0) return;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int px = tx * kTile + (warp & 1) * 8 + (lane & 7);
+    const int py = ty * kTile + (warp >> 1) * 4 + (lane >> 3);
+    const bool in_fb = px < A.dims.width && py < A.dims.height;
+    const size_t pix = (size_t)py * A.dims.width + px;
+
+    // buffers a clear fully covers are never loaded
+    const int bx0 = tx * kTile, by0 = ty * kTile;
+    const int bx1 = min(bx0 + kTile, A.dims.width), by1 = min(by0 + kTile, A.dims.height);
+    bool load_c = true, load_d = true, load_s = true;
+    for (int i = 0; i < A.nclears; i++) {
+        const ClearOp &c = A.clears[i];
+        if (covers_tile(c, GL_COLOR_BUFFER_BIT, bx0, by0, bx1, by1)) load_c = false;
+        if (covers_tile(c, GL_DEPTH_BUFFER_BIT, bx0, by0, bx1, by1)) load_d = false;
+        if (covers_tile(c, GL_STENCIL_BUFFER_BIT, bx0, by0, bx1, by1)) load_s = false;
+    }
+    uint32_t col = 0, st = 0;
+    float dep = 1.0f;
+    if (in_fb) {
+        if (load_c) col = A.color[pix];
+        if (load_d) dep = A.depth[pix];
+        if (load_s) st = A.stencil[pix];
+        for (int i = 0; i < A.nclears; i++) {
+            const ClearOp &c = A.clears[i];
+            if (px >= c.x0 && px < c.x1 && py >= c.y0 && py < c.y1) {
+                if (c.mask & GL_COLOR_BUFFER_BIT) col = c.color;
+                if (c.mask & GL_DEPTH_BUFFER_BIT) dep = c.depth;
+                if (c.mask & GL_STENCIL_BUFFER_BIT) st = c.stencil & 0xFFu;
+            }
+        }
+    }
+
+    const float fpx = (float)px, fpy = (float)py;
+    const uint32_t start = A.tile_start[tile];
+    uint32_t frags = 0;
+    const bool have_eye = A.eye_records != nullptr;
+
+    for (uint32_t base = 0; base < count; base += kChunk) {
+        const int n = (int)min((uint32_t)kChunk, count - base);
+        __syncthreads();
+        for (int i = threadIdx.x; i < n * (kRecWords / 4); i += kTileThreads) {
+            const int r = i / (kRecWords / 4), q = i % (kRecWords / 4);
+            const uint32_t idx = __ldg(A.tile_vals + start + base + r);
+            s_rec[r][q] = __ldg(reinterpret_cast<const float4 *>(A.records) + (size_t)idx * (kRecWords / 4) + q);
+        }
+        if (have_eye) {
+            for (int i = threadIdx.x; i < n * (kEyeWords / 4); i += kTileThreads) {
+                const int r = i / (kEyeWords / 4), q = i % (kEyeWords / 4);
+                const uint32_t idx = __ldg(A.tile_vals + start + base + r);
+                s_eye[r][q] = __ldg(reinterpret_cast<const float4 *>(A.eye_records) + (size_t)idx * (kEyeWords / 4) + q);
+            }
+        }
+        __syncthreads();
+        if (!in_fb) continue;
+
+        for (int j = 0; j < n; j++) {
+            const float *r = reinterpret_cast<const float *>(s_rec[j]);
+            if (px < __float_as_int(r[R_MINX]) || px > __float_as_int(r[R_MAXX]) || py < __float_as_int(r[R_MINY]) ||
+                py > __float_as_int(r[R_MAXY]))
+                continue;
+            const float x0 = r[R_X0], y0 = r[R_Y0], x1 = r[R_X1], y1 = r[R_Y1], x2 = r[R_X2], y2 = r[R_Y2];
+            // edge_function at the integer pixel position (raster.c:299-302, 534-536)
+            const float e0 = (fpx - x1) * (y2 - y1) - (fpy - y1) * (x2 - x1);
+            const float e1 = (fpx - x2) * (y0 - y2) - (fpy - y2) * (x0 - x2);
+            const float e2 = (fpx - x0) * (y1 - y0) - (fpy - y0) * (x1 - x0);
+            const float area = r[R_AREA];
+            if (!((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) || (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0)))
+                continue;
+            frags++;
+            const float inv_area = r[R_INV_AREA];
+            const float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
+            const DevRaster &R = A.rasters[min(__float_as_uint(r[R_RASTER]), A.nrasters - 1)];
+            const mtgl_raster_state &rs = R.rs;
+            const float z = b0 * r[R_Z0] + b1 * r[R_Z1] + b2 * r[R_Z2];
+            const float depth = map_depth(R, z);
+
+            uint32_t sv = 0;
+            if (rs.stencil_test) {
+                sv = st;
+                if (!stencil_pass(rs.stencil_func, rs.stencil_ref, rs.stencil_mask, sv)) {
+                    st = stencil_write(st, stencil_apply(rs.stencil_fail, sv, rs.stencil_ref), rs.stencil_writemask);
+                    continue;
+                }
+            }
+            if (rs.depth_test && !cmp_pass(rs.depth_func, depth, dep)) {
+                if (rs.stencil_test)
+                    st = stencil_write(st, stencil_apply(rs.stencil_zfail, sv, rs.stencil_ref), rs.stencil_writemask);
+                continue;
+            }
+            if (rs.stencil_test)
+                st = stencil_write(st, stencil_apply(rs.stencil_zpass, sv, rs.stencil_ref), rs.stencil_writemask);
+
+            float4 c;
+            if (rs.shade_model == GL_FLAT) {
+                c = make_float4(r[R_C2], r[R_C2 + 1], r[R_C2 + 2], r[R_C2 + 3]);
+            } else {
+                c = make_float4(r[R_C0] * b0 + r[R_C1] * b1 + r[R_C2] * b2,
+                                r[R_C0 + 1] * b0 + r[R_C1 + 1] * b1 + r[R_C2 + 1] * b2,
+                                r[R_C0 + 2] * b0 + r[R_C1 + 2] * b1 + r[R_C2 + 2] * b2,
+                                r[R_C0 + 3] * b0 + r[R_C1 + 3] * b1 + r[R_C2 + 3] * b2);
+            }
+            if (rs.lighting && have_eye) {
+                const bool back = (__float_as_uint(r[R_FLAGS]) & 1u) != 0;
+                const bool phong = rs.shade_model == GL_PHONG;
+                if (phong || (back && rs.lit.two_side)) {
+                    const float *e = reinterpret_cast<const float *>(s_eye[j]);
+                    float3 ep = make_float3(e[0] * b0 + e[6] * b1 + e[12] * b2, e[1] * b0 + e[7] * b1 + e[13] * b2,
+                                            e[2] * b0 + e[8] * b1 + e[14] * b2);
+                    float3 en = make_float3(e[3] * b0 + e[9] * b1 + e[15] * b2, e[4] * b0 + e[10] * b1 + e[16] * b2,
+                                            e[5] * b0 + e[11] * b1 + e[17] * b2);
+                    const mtgl_material *mat = &rs.lit.front;
+                    if (back && rs.lit.two_side) {
+                        en = make_float3(en.x * -1.0f, en.y * -1.0f, en.z * -1.0f);
+                        mat = &rs.lit.back;
+                    }
+                    c = compute_lighting(rs.lit, ep, en, *mat);
+                }
+            }
+            if (R.tex) {
+                float u, v;
+                if (rs.perspective_hint != GL_FASTEST) {
+                    const float uow = b0 * r[R_UW0] + b1 * r[R_UW1] + b2 * r[R_UW2];
+                    const float vow = b0 * r[R_VW0] + b1 * r[R_VW1] + b2 * r[R_VW2];
+                    const float oow = b0 * r[R_W0] + b1 * r[R_W1] + b2 * r[R_W2];
+                    const float w = 1.0f / oow;
+                    u = uow * w;
+                    v = vow * w;
+                } else {
+                    u = b0 * r[R_UV0] + b1 * r[R_UV1] + b2 * r[R_UV2];
+                    v = b0 * r[R_UV0 + 1] + b1 * r[R_UV1 + 1] + b2 * r[R_UV2 + 1];
+                }
+                const float4 tc = unpack_rgba(sample_lod(R, u, v, r[R_LOD]));
+                // the alpha test applies to textured fragments only (raster.c:639-643)
+                if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) continue;
+                switch (rs.tex_env_mode) {
+                case GL_REPLACE: c = tc; break;
+                case GL_DECAL: c = lerp_rgb(c, tc, tc.w); break;
+                case GL_BLEND:
+                    c = make_float4(c.x * (1.0f - tc.x) + rs.tex_env_color[0] * tc.x,
+                                    c.y * (1.0f - tc.y) + rs.tex_env_color[1] * tc.y,
+                                    c.z * (1.0f - tc.z) + rs.tex_env_color[2] * tc.z, c.w * tc.w);
+                    break;
+                case GL_ADD: c = make_float4(c.x + tc.x, c.y + tc.y, c.z + tc.z, c.w * tc.w); break;
+                default: c = make_float4(c.x * tc.x, c.y * tc.y, c.z * tc.z, c.w * tc.w); break;
+                }
+            }
+            if (rs.fog) {
+                const float fc = b0 * r[R_EZ0] + b1 * r[R_EZ1] + b2 * r[R_EZ2];
+                c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, fc));
+            }
+            if (rs.depth_test && rs.depth_mask) dep = depth;
+            if (rs.blend) c = blend(rs, c, unpack_rgba(col));
+            c = clamp4(c);
+            col = masked_write(rs, col, c);
+        }
+    }
+
+    if (in_fb) {
+        A.color[pix] = col;
+        A.depth[pix] = dep;
+        A.stencil[pix] = (uint8_t)st;
+    }
+    if (A.fragments) {
+        uint32_t f = __reduce_add_sync(0xffffffffu, frags);
+        if (lane == 0 && f) atomicAdd(A.fragments, (unsigned long long)f);
+    }
+}
+
+int launch_tile(const TileArgs &a, cudaStream_t s)
+{
+    const int ntiles = a.dims.tiles_x * a.dims.tiles_y;
+    if (ntiles == 0) return 0;
+    k_tile<<<ntiles, kTileThreads, 0, s>>>(a);
+    return 1;
+}
+
+}  // namespace mtgl

@@ -1,0 +1,442 @@
+// mtgl_device.cuh — device-side data layout and arithmetic of the GB300 back end.
+//
+// Every float expression here reproduces the reference's operation order (src/graphics.h,
+// src/lighting.h, src/raster.c, src/textures.c) and the translation units are compiled
+// with -fmad=false and IEEE division/square root, so each result is the value the
+// reference computes on x86-64. Float->int conversions emulate x86-64 cvttss2si (NaN and
+// out-of-range give INT32_MIN), which is what the reference's casts compile to.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "GL/gl.h"
+#include "mytinygl/mtgl_dev.h"
+
+namespace mtgl {
+
+// ------------------------------------------------------------------ layout constants
+
+constexpr int kTile = 16;            // tile edge in pixels (one CTA per tile)
+constexpr int kTileThreads = kTile * kTile;
+constexpr int kRecWords = 48;        // words per triangle record
+constexpr int kEyeWords = 20;        // words per triangle eye-space record (per-fragment lighting)
+
+// Triangle record written by the setup kernel, read by the tile kernel (raster.c:451-529
+// inputs plus the per-triangle values rasterize_triangle_smooth derives before its loop).
+enum RecField {
+    R_X0 = 0, R_Y0, R_X1, R_Y1, R_X2, R_Y2,   // screen vertices as floats of the int coordinates
+    R_MINX = 6, R_MINY, R_MAXX, R_MAXY,       // int32 bbox after viewport/scissor/framebuffer clamps
+    R_AREA = 10, R_INV_AREA,
+    R_Z0 = 12, R_Z1, R_Z2,
+    R_W0 = 15, R_W1, R_W2,                    // 1/w
+    R_C0 = 18, R_C1 = 22, R_C2 = 26,          // RGBA each
+    R_UV0 = 30, R_UV1 = 32, R_UV2 = 34,       // raw texcoords
+    R_UW0 = 36, R_VW0, R_UW1, R_VW1, R_UW2, R_VW2,
+    R_EZ0 = 42, R_EZ1, R_EZ2,
+    R_LOD = 45,
+    R_RASTER = 46,                            // uint32 raster-state index
+    R_FLAGS = 47                              // bit 0: back facing
+};
+
+// Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).
+struct __align__(16) PostVertex {
+    float4 clip;
+    float4 color;
+    float2 uv;
+    float eye_z;
+    float pad;
+};
+struct __align__(16) PostEye {
+    float4 pos_nx;   // eye_pos.xyz, eye_normal.x
+    float4 nyz;      // eye_normal.y, eye_normal.z
+};
+
+struct DevAttrib {
+    const uint8_t *ptr;   // element `base_index` is at ptr
+    int64_t base_index;
+    uint64_t bytes;       // readable bytes from ptr
+    int32_t size, type, stride, enabled;
+};
+
+// One draw packet as the kernels see it.
+struct DevDraw {
+    uint32_t mode;
+    int32_t first, count;
+    uint32_t index_type;
+    const uint8_t *indices;
+    int64_t index_min;
+    int32_t range_n;       // range mode: vertices index_min .. index_min+range_n-1
+    int32_t range_mode;    // 1: slots cover an index range (+1 default slot), 0: one slot per element
+    int32_t pos2d;
+    DevAttrib pos, color, tex, normal;
+    float cur_color[4], cur_tex[2], cur_normal[3];
+    const uint32_t *vs_ids;
+    uint32_t vs_base;
+    uint32_t raster;
+    uint32_t vslot_base, vslot_count;
+    uint32_t tri_base, tri_count;
+};
+
+// Raster state with the bound texture resolved to device pointers.
+struct DevRaster {
+    mtgl_raster_state rs;
+    const uint32_t *tex;   // level 0, or null when texturing is off
+    const uint32_t *mip1;  // level 1, or null when the reference cannot build it (w or h < 2)
+    int32_t tex_w, tex_h, mip_w, mip_h;
+    int32_t default_depth_range;
+    int32_t needs_eye;     // per-fragment lighting reads eye-space interpolants
+};
+
+struct ClearOp {
+    uint32_t mask;
+    int32_t x0, y0, x1, y1;
+    uint32_t color;
+    float depth;
+    uint32_t stencil;
+};
+
+struct FrameDims {
+    int32_t width, height;
+    int32_t tiles_x, tiles_y;
+};
+
+// ------------------------------------------------------------------ scalar helpers
+
+__device__ __forceinline__ int32_t x86_f2i(float f)
+{
+    return (f >= -2147483648.0f && f < 2147483648.0f) ? (int32_t)f : INT32_MIN;
+}
+
+__device__ __forceinline__ float u8f(uint32_t v) { return (float)v / 255.0f; }
+
+// color_to_rgba32 (graphics.h:337-348)
+__device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a)
+{
+    float rf = r < 0.0f ? 0.0f : (r > 1.0f ? 1.0f : r);
+    float gf = g < 0.0f ? 0.0f : (g > 1.0f ? 1.0f : g);
+    float bf = b < 0.0f ? 0.0f : (b > 1.0f ? 1.0f : b);
+    float af = a < 0.0f ? 0.0f : (a > 1.0f ? 1.0f : a);
+    uint32_t ri = (uint32_t)x86_f2i(rf * 255.0f) & 0xFFu;
+    uint32_t gi = (uint32_t)x86_f2i(gf * 255.0f) & 0xFFu;
+    uint32_t bi = (uint32_t)x86_f2i(bf * 255.0f) & 0xFFu;
+    uint32_t ai = (uint32_t)x86_f2i(af * 255.0f) & 0xFFu;
+    return (ai << 24) | (bi << 16) | (gi << 8) | ri;
+}
+
+__device__ __forceinline__ float4 unpack_rgba(uint32_t p)
+{
+    return make_float4(u8f(p & 0xFFu), u8f((p >> 8) & 0xFFu), u8f((p >> 16) & 0xFFu), u8f((p >> 24) & 0xFFu));
+}
+
+__device__ __forceinline__ float clamp01(float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); }
+__device__ __forceinline__ float4 clamp4(float4 c)
+{
+    return make_float4(clamp01(c.x), clamp01(c.y), clamp01(c.z), clamp01(c.w));
+}
+
+// color_lerp (graphics.h:293-296): a*(1-t) + b*t
+__device__ __forceinline__ float4 lerp_col(float4 a, float4 b, float t)
+{
+    float s = 1.0f - t;
+    return make_float4(a.x * s + b.x * t, a.y * s + b.y * t, a.z * s + b.z * t, a.w * s + b.w * t);
+}
+
+// color_lerp_rgb (graphics.h:298-305): a + (b-a)*t, keeps a's alpha
+__device__ __forceinline__ float4 lerp_rgb(float4 a, float4 b, float t)
+{
+    return make_float4(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t, a.w);
+}
+
+__device__ __forceinline__ float3 normalize3(float x, float y, float z)
+{
+    float len = sqrtf(x * x + y * y + z * z);
+    if (len > 0.0f) {
+        float s = 1.0f / len;
+        return make_float3(x * s, y * s, z * s);
+    }
+    return make_float3(x, y, z);
+}
+
+// mat4_mul_vec4 (graphics.h:131-138), column-major m
+__device__ __forceinline__ float4 mul_m4(const float *m, float x, float y, float z, float w)
+{
+    return make_float4(m[0] * x + m[4] * y + m[8] * z + m[12] * w, m[1] * x + m[5] * y + m[9] * z + m[13] * w,
+                       m[2] * x + m[6] * y + m[10] * z + m[14] * w, m[3] * x + m[7] * y + m[11] * z + m[15] * w);
+}
+
+__device__ __forceinline__ bool cmp_pass(uint32_t func, float a, float b)
+{
+    switch (func) {
+    case GL_NEVER: return false;
+    case GL_LESS: return a < b;
+    case GL_EQUAL: return a == b;
+    case GL_LEQUAL: return a <= b;
+    case GL_GREATER: return a > b;
+    case GL_NOTEQUAL: return a != b;
+    case GL_GEQUAL: return a >= b;
+    default: return true;
+    }
+}
+
+// ------------------------------------------------------------------ lighting (lighting.h:53-142)
+
+__device__ __forceinline__ float4 ld4(const float *p) { return make_float4(p[0], p[1], p[2], p[3]); }
+
+__device__ inline float4 compute_lighting(const mtgl_lighting &L, float3 ep, float3 en, const mtgl_material &mat)
+{
+    // emission + ambient * global ambient, alpha from the diffuse material
+    float4 r = make_float4(mat.emission[0] + mat.ambient[0] * L.model_ambient[0],
+                           mat.emission[1] + mat.ambient[1] * L.model_ambient[1],
+                           mat.emission[2] + mat.ambient[2] * L.model_ambient[2],
+                           mat.emission[3] + mat.ambient[3] * L.model_ambient[3]);
+    r.w = mat.diffuse[3];
+    float3 N = en;
+    if (L.normalize) N = normalize3(N.x, N.y, N.z);
+    for (int i = 0; i < MTGL_MAX_LIGHTS; i++) {
+        const mtgl_light &l = L.lights[i];
+        if (!l.enabled) continue;
+        float3 Ld;
+        float att = 1.0f;
+        if (l.position[3] == 0.0f) {
+            Ld = make_float3(l.dir_normalized[0], l.dir_normalized[1], l.dir_normalized[2]);
+        } else {
+            float tx = l.position[0] - ep.x, ty = l.position[1] - ep.y, tz = l.position[2] - ep.z;
+            float dist = sqrtf(tx * tx + ty * ty + tz * tz);
+            if (dist < 1e-6f) dist = 1e-6f;
+            float inv = 1.0f / dist;
+            Ld = make_float3(tx * inv, ty * inv, tz * inv);
+            float den = l.constant_attenuation + l.linear_attenuation * dist + l.quadratic_attenuation * dist * dist;
+            if (den < 1e-6f) den = 1e-6f;
+            att = 1.0f / den;
+            if (l.spot_cutoff < 180.0f) {
+                float ca = -(Ld.x * l.spot_dir_normalized[0] + Ld.y * l.spot_dir_normalized[1] +
+                             Ld.z * l.spot_dir_normalized[2]);
+                if (ca < l.cos_cutoff) att = 0.0f;
+                else att *= powf(ca, l.spot_exponent);
+            }
+        }
+        if (att <= 0.0f) continue;
+        r.x = r.x + (mat.ambient[0] * l.ambient[0]) * att;
+        r.y = r.y + (mat.ambient[1] * l.ambient[1]) * att;
+        r.z = r.z + (mat.ambient[2] * l.ambient[2]) * att;
+        r.w = r.w + (mat.ambient[3] * l.ambient[3]) * att;
+        float ndl = N.x * Ld.x + N.y * Ld.y + N.z * Ld.z;
+        if (ndl > 0.0f) {
+            float k = att * ndl;
+            r.x = r.x + (mat.diffuse[0] * l.diffuse[0]) * k;
+            r.y = r.y + (mat.diffuse[1] * l.diffuse[1]) * k;
+            r.z = r.z + (mat.diffuse[2] * l.diffuse[2]) * k;
+            r.w = r.w + (mat.diffuse[3] * l.diffuse[3]) * k;
+            if (mat.shininess > 0.0f) {
+                float3 V = L.local_viewer ? normalize3(ep.x * -1.0f, ep.y * -1.0f, ep.z * -1.0f)
+                                          : make_float3(0.0f, 0.0f, 1.0f);
+                float3 Hh = normalize3(Ld.x + V.x, Ld.y + V.y, Ld.z + V.z);
+                float ndh = N.x * Hh.x + N.y * Hh.y + N.z * Hh.z;
+                if (ndh > 0.0f) {
+                    float sp = powf(ndh, mat.shininess) * att;
+                    r.x = r.x + (mat.specular[0] * l.specular[0]) * sp;
+                    r.y = r.y + (mat.specular[1] * l.specular[1]) * sp;
+                    r.z = r.z + (mat.specular[2] * l.specular[2]) * sp;
+                    r.w = r.w + (mat.specular[3] * l.specular[3]) * sp;
+                }
+            }
+        }
+    }
+    return clamp4(r);
+}
+
+// ------------------------------------------------------------------ texture sampling (textures.c:271-557)
+
+struct TexView {
+    const uint32_t *px;
+    int32_t w, h;
+};
+
+__device__ __forceinline__ uint32_t texel_wrapped(const TexView &t, int32_t ws, int32_t wt, int32_t x, int32_t y)
+{
+    if (ws == GL_REPEAT) x = ((x % t.w) + t.w) % t.w;
+    else { if (x < 0) x = 0; else if (x >= t.w) x = t.w - 1; }
+    if (wt == GL_REPEAT) y = ((y % t.h) + t.h) % t.h;
+    else { if (y < 0) y = 0; else if (y >= t.h) y = t.h - 1; }
+    return __ldg(t.px + (size_t)y * t.w + x);
+}
+
+__device__ __forceinline__ uint32_t sample_level(const TexView &t, int32_t ws, int32_t wt, float u, float v, bool linear)
+{
+    float tx = u * (float)t.w - 0.5f;
+    float ty = v * (float)t.h - 0.5f;
+    if (linear) {
+        int32_t x0 = x86_f2i(floorf(tx)), y0 = x86_f2i(floorf(ty));
+        float fx = tx - (float)x0, fy = ty - (float)y0;
+        float4 c00 = unpack_rgba(texel_wrapped(t, ws, wt, x0, y0));
+        float4 c10 = unpack_rgba(texel_wrapped(t, ws, wt, x0 + 1, y0));
+        float4 c01 = unpack_rgba(texel_wrapped(t, ws, wt, x0, y0 + 1));
+        float4 c11 = unpack_rgba(texel_wrapped(t, ws, wt, x0 + 1, y0 + 1));
+        float4 top = lerp_col(c00, c10, fx);
+        float4 bot = lerp_col(c01, c11, fx);
+        float4 r = lerp_col(top, bot, fy);
+        return pack_rgba(r.x, r.y, r.z, r.w);
+    }
+    int32_t x = x86_f2i(floorf(tx + 0.5f)), y = x86_f2i(floorf(ty + 0.5f));
+    if (x < 0) x = 0;
+    if (x >= t.w) x = t.w - 1;
+    if (y < 0) y = 0;
+    if (y >= t.h) y = t.h - 1;
+    return __ldg(t.px + (size_t)y * t.w + x);
+}
+
+__device__ __forceinline__ uint32_t sample_mip1(const DevRaster &R, float u, float v, int32_t filter)
+{
+    if (!R.mip1) return 0xFFFFFFFFu;  // level 1 cannot be built (textures.c:317, 416-419)
+    TexView m{R.mip1, R.mip_w, R.mip_h};
+    bool lin = filter == GL_LINEAR || filter == GL_LINEAR_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_LINEAR;
+    return sample_level(m, R.rs.tex_wrap_s, R.rs.tex_wrap_t, u, v, lin);
+}
+
+__device__ inline uint32_t sample_lod(const DevRaster &R, float u, float v, float lod)
+{
+    const int32_t ws = R.rs.tex_wrap_s, wt = R.rs.tex_wrap_t;
+    if (ws == GL_REPEAT) {
+        u = u - (float)x86_f2i(u);
+        if (u < 0) u += 1.0f;
+    } else {
+        if (u < 0.0f) u = 0.0f;
+        if (u > 1.0f) u = 1.0f;
+    }
+    if (wt == GL_REPEAT) {
+        v = v - (float)x86_f2i(v);
+        if (v < 0) v += 1.0f;
+    } else {
+        if (v < 0.0f) v = 0.0f;
+        if (v > 1.0f) v = 1.0f;
+    }
+    int32_t filter = (lod > 0.0f) ? R.rs.tex_min_filter : R.rs.tex_mag_filter;
+    TexView base{R.tex, R.tex_w, R.tex_h};
+    if (filter == GL_NEAREST_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_NEAREST) {
+        if (lod >= 0.5f) return sample_mip1(R, u, v, filter);
+        filter = (filter == GL_NEAREST_MIPMAP_NEAREST) ? GL_NEAREST : GL_LINEAR;
+    } else if (filter == GL_NEAREST_MIPMAP_LINEAR || filter == GL_LINEAR_MIPMAP_LINEAR) {
+        if (lod > 0.0f) {
+            float cl = (lod > 1.0f) ? 1.0f : lod;
+            uint32_t c0 = sample_level(base, ws, wt, u, v, filter == GL_LINEAR_MIPMAP_LINEAR);
+            uint32_t c1 = sample_mip1(R, u, v, filter);
+            float4 r = lerp_col(unpack_rgba(c0), unpack_rgba(c1), cl);
+            return pack_rgba(r.x, r.y, r.z, r.w);
+        }
+        filter = (filter == GL_NEAREST_MIPMAP_LINEAR) ? GL_NEAREST : GL_LINEAR;
+    }
+    return sample_level(base, ws, wt, u, v, filter == GL_LINEAR);
+}
+
+// ------------------------------------------------------------------ fragment helpers (raster.c:343-448, 672-705)
+
+__device__ __forceinline__ float4 blend_factor(uint32_t f, float4 s, float4 d)
+{
+    switch (f) {
+    case GL_ZERO: return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    case GL_ONE: return make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    case GL_SRC_COLOR: return s;
+    case GL_ONE_MINUS_SRC_COLOR: return make_float4(1 - s.x, 1 - s.y, 1 - s.z, 1 - s.w);
+    case GL_DST_COLOR: return d;
+    case GL_ONE_MINUS_DST_COLOR: return make_float4(1 - d.x, 1 - d.y, 1 - d.z, 1 - d.w);
+    case GL_SRC_ALPHA: return make_float4(s.w, s.w, s.w, s.w);
+    case GL_ONE_MINUS_SRC_ALPHA: { float k = 1 - s.w; return make_float4(k, k, k, k); }
+    case GL_DST_ALPHA: return make_float4(d.w, d.w, d.w, d.w);
+    case GL_ONE_MINUS_DST_ALPHA: { float k = 1 - d.w; return make_float4(k, k, k, k); }
+    case GL_SRC_ALPHA_SATURATE: {
+        float k = (s.w < (1 - d.w)) ? s.w : (1 - d.w);
+        return make_float4(k, k, k, 1.0f);
+    }
+    default: return make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    }
+}
+
+__device__ __forceinline__ float4 blend(const mtgl_raster_state &rs, float4 s, float4 d)
+{
+    float4 sf = blend_factor(rs.blend_src, s, d);
+    float4 df = blend_factor(rs.blend_dst, s, d);
+    return clamp4(make_float4(s.x * sf.x + d.x * df.x, s.y * sf.y + d.y * df.y, s.z * sf.z + d.z * df.z,
+                              s.w * sf.w + d.w * df.w));
+}
+
+__device__ __forceinline__ bool stencil_pass(uint32_t func, int32_t ref, uint32_t mask, uint32_t val)
+{
+    int32_t mr = (int32_t)((uint32_t)ref & mask);
+    int32_t mv = (int32_t)(val & mask);
+    switch (func) {
+    case GL_NEVER: return false;
+    case GL_LESS: return mr < mv;
+    case GL_EQUAL: return mr == mv;
+    case GL_LEQUAL: return mr <= mv;
+    case GL_GREATER: return mr > mv;
+    case GL_NOTEQUAL: return mr != mv;
+    case GL_GEQUAL: return mr >= mv;
+    default: return true;
+    }
+}
+
+__device__ __forceinline__ uint32_t stencil_apply(uint32_t op, uint32_t v, int32_t ref)
+{
+    switch (op) {
+    case GL_KEEP: return v;
+    case GL_ZERO: return 0u;
+    case GL_REPLACE: return (uint32_t)ref & 0xFFu;
+    case GL_INCR: return v < 255u ? v + 1u : 255u;
+    case GL_INCR_WRAP: return (v + 1u) & 0xFFu;
+    case GL_DECR: return v > 0u ? v - 1u : 0u;
+    case GL_DECR_WRAP: return (v - 1u) & 0xFFu;
+    case GL_INVERT: return (~v) & 0xFFu;
+    default: return v;
+    }
+}
+
+__device__ __forceinline__ uint32_t stencil_write(uint32_t old, uint32_t nv, uint32_t writemask)
+{
+    uint32_t m8 = writemask & 0xFFu;
+    return ((old & ~m8) | (nv & m8)) & 0xFFu;
+}
+
+__device__ __forceinline__ float fog_factor(const mtgl_raster_state &rs, float fog_coord)
+{
+    float f;
+    switch (rs.fog_mode) {
+    case GL_LINEAR:
+        f = (rs.fog_end != rs.fog_start) ? (rs.fog_end - fog_coord) / (rs.fog_end - rs.fog_start) : 1.0f;
+        break;
+    case GL_EXP: f = expf(-rs.fog_density * fog_coord); break;
+    case GL_EXP2: {
+        float d = rs.fog_density * fog_coord;
+        f = expf(-d * d);
+        break;
+    }
+    default: f = 1.0f; break;
+    }
+    if (f < 0.0f) f = 0.0f;
+    if (f > 1.0f) f = 1.0f;
+    return f;
+}
+
+// depth range mapping (raster.c:548): float NDC term, double range, float result
+__device__ __forceinline__ float map_depth(const DevRaster &R, float z)
+{
+    float t = (z + 1.0f) * 0.5f;
+    if (R.default_depth_range) return t;  // (double)t * 1.0 + 0.0 rounds back to t
+    return (float)((double)t * (R.rs.depth_far - R.rs.depth_near) + R.rs.depth_near);
+}
+
+// write_pixel_masked (raster.c:20-45) on a packed destination pixel
+__device__ __forceinline__ uint32_t masked_write(const mtgl_raster_state &rs, uint32_t dst, float4 c)
+{
+    const uint32_t *m = rs.color_mask;
+    if (m[0] && m[1] && m[2] && m[3]) return pack_rgba(c.x, c.y, c.z, c.w);
+    if (!m[0] && !m[1] && !m[2] && !m[3]) return dst;
+    float4 d = unpack_rgba(dst);
+    if (m[0]) d.x = c.x;
+    if (m[1]) d.y = c.y;
+    if (m[2]) d.z = c.z;
+    if (m[3]) d.w = c.w;
+    return pack_rgba(d.x, d.y, d.z, d.w);
+}
+
+}  // namespace mtgl

@@ -175,6 +175,12 @@ int mtgl_framebuffer_size(GLState *c, int32_t *w, int32_t *h)
 
 const char *mtgl_backend_name(void) { return mtgl_dev_backend_name(); }
 
+int mtgl_get_stats(GLState *c, mtgl_stats *out) { return c ? mtgl_dev_stats(c->dev, out) : MTGL_ERR_INVALID; }
+int mtgl_reset_stats(GLState *c) { return c ? mtgl_dev_reset_stats(c->dev) : MTGL_ERR_INVALID; }
+int mtgl_set_profiling(GLState *c, int enable) { return c ? mtgl_dev_profile(c->dev, enable) : MTGL_ERR_INVALID; }
+int mtgl_get_timings(GLState *c, mtgl_timings *out) { return c ? mtgl_dev_timings(c->dev, out) : MTGL_ERR_INVALID; }
+void *mtgl_cuda_stream(GLState *c) { return c ? mtgl_dev_stream(c->dev) : NULL; }
+
 /* ---- capabilities (gl_api.c:351-407) ---- */
 static uint32_t cap_flag(GLenum cap)
 {

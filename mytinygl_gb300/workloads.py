@@ -61,6 +61,15 @@ def uv_sphere(stacks=32, slices=32, radius=1.0):
     return (p * radius).astype(np.float32), nrm.astype(np.float32), np.array(idx, np.uint32)
 
 
+def frame_start(scene: Scene) -> int:
+    """Index of the first call of the per-frame part (the first glClear): everything before
+    it uploads resident inputs (buffers, textures) once."""
+    for i, (name, _) in enumerate(scene.cmds):
+        if name == "glClear":
+            return i
+    return 0
+
+
 def _vbo(s: Scene, target, data: np.ndarray, buf_id: int):
     s.glBindBuffer(target, buf_id)
     s.glBufferData(target, int(data.nbytes), data, G.GL_STATIC_DRAW)
@@ -75,8 +84,18 @@ def sphere_scene(width=800, height=600, seed=0, use_vbo=True, near=0.1, far=100.
     ang = rng.uniform(0.0, 2 * math.pi, 3)
     pos, nrm, idx = uv_sphere(stacks, slices)
     s = Scene("sphere", width, height)
+    if use_vbo:
+        # resident inputs, uploaded before the frame: one interleaved position+normal buffer
+        # (24-byte records; the array-buffer binding is read at draw time, so one buffer
+        # serves both pointers) and an element buffer
+        s.glGenBuffers(2, np.zeros(2, np.uint32))
+        inter = np.ascontiguousarray(np.concatenate([pos, nrm], axis=1).astype(np.float32))
+        _vbo(s, G.GL_ARRAY_BUFFER, inter, 1)
+        _vbo(s, G.GL_ELEMENT_ARRAY_BUFFER, idx, 2)
     s.glViewport(0, 0, width, height)
     s.glClearColor(0.0, 0.0, 0.0, 1.0)
+    # ---- frame
+    s.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT)
     s.glMatrixMode(G.GL_PROJECTION)
     s.glLoadIdentity()
     s.glFrustum(*frustum_params(60.0, width / height, near, far))
@@ -93,18 +112,13 @@ def sphere_scene(width=800, height=600, seed=0, use_vbo=True, near=0.1, far=100.
     s.glCullFace(G.GL_BACK)
     s.glTranslatef(0.0, 0.0, -3.0)
     s.glMultMatrixf(euler_matrix(*ang))
-    s.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT)
     s.glEnableClientState(G.GL_VERTEX_ARRAY)
     s.glEnableClientState(G.GL_NORMAL_ARRAY)
     if use_vbo:
-        # the array-buffer binding is read at draw time, so positions and normals share one
-        # interleaved buffer (24-byte records); indices live in an element buffer
-        s.glGenBuffers(2, np.zeros(2, np.uint32))
-        inter = np.ascontiguousarray(np.concatenate([pos, nrm], axis=1).astype(np.float32))
-        _vbo(s, G.GL_ARRAY_BUFFER, inter, 1)
+        s.glBindBuffer(G.GL_ARRAY_BUFFER, 1)
+        s.glBindBuffer(G.GL_ELEMENT_ARRAY_BUFFER, 2)
         s.glVertexPointer(3, G.GL_FLOAT, 24, 0)
         s.glNormalPointer(G.GL_FLOAT, 24, 12)
-        _vbo(s, G.GL_ELEMENT_ARRAY_BUFFER, idx, 2)
         s.glDrawElements(G.GL_TRIANGLES, int(idx.size), G.GL_UNSIGNED_INT, 0)
     else:
         s.glVertexPointer(3, G.GL_FLOAT, 0, pos)
@@ -143,16 +157,26 @@ def textured_scene(width=1920, height=1080, ntri=100_000, seed=1, tex_size=512, 
     lcol = rng.uniform(0.2, 1.0, (lights, 3)).astype(np.float32)
 
     s = Scene("textured", width, height)
-    s.glViewport(0, 0, width, height)
-    s.glClearColor(0.1, 0.1, 0.2, 1.0)
-    s.glMatrixMode(G.GL_PROJECTION)
-    s.glLoadIdentity()
-    s.glMatrixMode(G.GL_MODELVIEW)
-    s.glLoadIdentity()
     s.glGenTextures(1, np.zeros(1, np.uint32))
     s.glBindTexture(G.GL_TEXTURE_2D, 1)
     s.glTexImage2D(G.GL_TEXTURE_2D, 0, G.GL_RGBA, tex_size, tex_size, 0, G.GL_RGBA, G.GL_UNSIGNED_BYTE,
                    np.ascontiguousarray(tex))
+    if use_vbo:
+        # resident inputs: one interleaved buffer pos f32x3 | colour u8x4 | uv f32x2 | normal f32x3 (36 B)
+        rec = np.zeros(ntri * 3, dtype=[("p", "<f4", 3), ("c", "u1", 4), ("t", "<f4", 2), ("n", "<f4", 3)])
+        rec["p"], rec["c"], rec["t"], rec["n"] = pos, col, uv, nrm
+        raw = np.frombuffer(rec.tobytes(), np.uint8)
+        s.glGenBuffers(1, np.zeros(1, np.uint32))
+        _vbo(s, G.GL_ARRAY_BUFFER, raw, 1)
+    s.glViewport(0, 0, width, height)
+    s.glClearColor(0.1, 0.1, 0.2, 1.0)
+    # ---- frame
+    s.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT)
+    s.glMatrixMode(G.GL_PROJECTION)
+    s.glLoadIdentity()
+    s.glMatrixMode(G.GL_MODELVIEW)
+    s.glLoadIdentity()
+    s.glBindTexture(G.GL_TEXTURE_2D, 1)
     s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MIN_FILTER, min_filter)
     s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MAG_FILTER, G.GL_LINEAR)
     s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_WRAP_S, G.GL_REPEAT)
@@ -177,16 +201,10 @@ def textured_scene(width=1920, height=1080, ntri=100_000, seed=1, tex_size=512, 
         s.glFogfv(G.GL_FOG_COLOR, np.array([0.5, 0.5, 0.6, 1.0], np.float32))
     s.glEnable(G.GL_DEPTH_TEST)
     s.glDepthFunc(G.GL_LESS)
-    s.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT)
     for a in (G.GL_VERTEX_ARRAY, G.GL_COLOR_ARRAY, G.GL_TEXTURE_COORD_ARRAY, G.GL_NORMAL_ARRAY):
         s.glEnableClientState(a)
     if use_vbo:
-        # one interleaved buffer: pos f32x3 | colour u8x4 | uv f32x2 | normal f32x3 (36 B)
-        rec = np.zeros(ntri * 3, dtype=[("p", "<f4", 3), ("c", "u1", 4), ("t", "<f4", 2), ("n", "<f4", 3)])
-        rec["p"], rec["c"], rec["t"], rec["n"] = pos, col, uv, nrm
-        raw = np.frombuffer(rec.tobytes(), np.uint8)
-        s.glGenBuffers(1, np.zeros(1, np.uint32))
-        _vbo(s, G.GL_ARRAY_BUFFER, raw, 1)
+        s.glBindBuffer(G.GL_ARRAY_BUFFER, 1)
         s.glVertexPointer(3, G.GL_FLOAT, 36, 0)
         s.glColorPointer(4, G.GL_UNSIGNED_BYTE, 36, 12)
         s.glTexCoordPointer(2, G.GL_FLOAT, 36, 16)
@@ -228,9 +246,17 @@ def rop_scene(width=1920, height=1080, ntri=1_000_000, seed=2, median_area=20.0,
     col = np.repeat(col, 3, axis=0)
 
     s = Scene("rop", width, height)
+    if use_vbo:
+        rec = np.zeros(ntri * 3, dtype=[("p", "<f4", 3), ("c", "u1", 4)])
+        rec["p"], rec["c"] = pos, col
+        raw = np.frombuffer(rec.tobytes(), np.uint8)
+        s.glGenBuffers(1, np.zeros(1, np.uint32))
+        _vbo(s, G.GL_ARRAY_BUFFER, raw, 1)
     s.glViewport(0, 0, width, height)
     s.glClearColor(0.0, 0.0, 0.0, 1.0)
     s.glClearStencil(0)
+    # ---- frame
+    s.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT | G.GL_STENCIL_BUFFER_BIT)
     s.glMatrixMode(G.GL_PROJECTION)
     s.glLoadIdentity()
     s.glMatrixMode(G.GL_MODELVIEW)
@@ -244,16 +270,11 @@ def rop_scene(width=1920, height=1080, ntri=1_000_000, seed=2, median_area=20.0,
     s.glStencilOp(G.GL_KEEP, G.GL_KEEP, G.GL_INCR)
     s.glEnable(G.GL_DEPTH_TEST)
     s.glDepthFunc(G.GL_LEQUAL)
-    s.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT | G.GL_STENCIL_BUFFER_BIT)
     s.glDepthMask(0)
     s.glEnableClientState(G.GL_VERTEX_ARRAY)
     s.glEnableClientState(G.GL_COLOR_ARRAY)
     if use_vbo:
-        rec = np.zeros(ntri * 3, dtype=[("p", "<f4", 3), ("c", "u1", 4)])
-        rec["p"], rec["c"] = pos, col
-        raw = np.frombuffer(rec.tobytes(), np.uint8)
-        s.glGenBuffers(1, np.zeros(1, np.uint32))
-        _vbo(s, G.GL_ARRAY_BUFFER, raw, 1)
+        s.glBindBuffer(G.GL_ARRAY_BUFFER, 1)
         s.glVertexPointer(3, G.GL_FLOAT, 16, 0)
         s.glColorPointer(4, G.GL_UNSIGNED_BYTE, 16, 12)
     else:

@@ -1358,3 +1358,23 @@ int mtgl_dev_reset_stats(mtgl_dev *d)
     memset(&d->stats, 0, sizeof(d->stats));
     return MTGL_OK;
 }
+
+int mtgl_dev_profile(mtgl_dev *d, int enable)
+{
+    (void)d;
+    (void)enable;
+    return MTGL_OK;
+}
+
+int mtgl_dev_timings(mtgl_dev *d, mtgl_timings *out)
+{
+    (void)d;
+    memset(out, 0, sizeof(*out));
+    return MTGL_OK;
+}
+
+void *mtgl_dev_stream(mtgl_dev *d)
+{
+    (void)d;
+    return NULL;
+}

@@ -31,3 +31,9 @@ int mtgl_framebuffer_size(GLState *ctx, int32_t *w, int32_t *h)
 const uint32_t *mtgl_color_buffer(GLState *ctx) { return ctx ? ctx->framebuffer.color : 0; }
 
 const char *mtgl_backend_name(void) { return "reference"; }
+
+int mtgl_get_stats(GLState *ctx, void *out) { (void)ctx; (void)out; return 1; }
+int mtgl_reset_stats(GLState *ctx) { (void)ctx; return 1; }
+int mtgl_set_profiling(GLState *ctx, int enable) { (void)ctx; (void)enable; return 1; }
+int mtgl_get_timings(GLState *ctx, void *out) { (void)ctx; (void)out; return 1; }
+void *mtgl_cuda_stream(GLState *ctx) { (void)ctx; return 0; }

@@ -1,0 +1,138 @@
+"""GPU parity: libmytinygl_gb300.so against the CPU oracle and the golden fixtures.
+
+Tolerance (BASELINE the benchmark spec): depth and stencil bit-exact (NaN payloads aside), RGBA8
+colour within 1 LSB per channel, identical glGetError. The colour slack covers CUDA's
+expf/log2f/powf against glibc's in fog factors, texture LOD and specular terms.
+"""
+import numpy as np
+import pytest
+
+import feature_scenes as F
+import harness
+from mytinygl_gb300 import gl as G
+from mytinygl_gb300 import workloads as W
+from mytinygl_gb300.scene import Scene, render
+
+pytestmark = pytest.mark.gpu
+
+TRI_SCENES = sorted(n for n, (b, flags) in F.SCENES.items() if "lines" not in flags)
+LINE_SCENES = sorted(n for n, (b, flags) in F.SCENES.items() if "lines" in flags)
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    return harness.product()
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    return harness.oracle()
+
+
+def check(gpu, oracle, scene, tol=1):
+    a = render(oracle, scene)
+    b = render(gpu, scene)
+    stats = harness.compare(a, b)
+    harness.assert_parity(stats, color_tol=tol, name=scene.name)
+    return stats
+
+
+@pytest.mark.parametrize("name", TRI_SCENES)
+def test_feature_scene(gpu, oracle, name):
+    check(gpu, oracle, F.SCENES[name][0]())
+
+
+@pytest.mark.parametrize("path", [p for p in harness.golden_files()
+                                  if not any(p.endswith(f"/{n}.npz") for n in LINE_SCENES)],
+                         ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_golden(gpu, path):
+    scene, expected, buffers = harness.load_golden(path)
+    stats = harness.compare(expected, render(gpu, scene), buffers)
+    harness.assert_parity(stats, color_tol=1, name=scene.name)
+
+
+def test_sphere_full_size(gpu, oracle):
+    check(gpu, oracle, W.sphere_scene())
+    check(gpu, oracle, W.sphere_scene(use_vbo=False, seed=7))
+
+
+def test_textured_reduced(gpu, oracle):
+    check(gpu, oracle, W.textured_scene(480, 270, ntri=6000))
+
+
+def test_rop_reduced(gpu, oracle):
+    check(gpu, oracle, W.rop_scene(480, 270, ntri=60000))
+
+
+def test_immediate_equals_arrays(gpu):
+    """The same triangles through glBegin/glEnd and through glDrawArrays give the same image."""
+    rng = np.random.default_rng(9)
+    pos = rng.uniform(-1.2, 1.2, (300, 3)).astype(np.float32)
+    col = rng.uniform(0, 1, (300, 4)).astype(np.float32)
+    a = F.base("imm", 128, 96, persp=False)
+    a.glEnable(G.GL_DEPTH_TEST)
+    a.glBegin(G.GL_TRIANGLES)
+    for p, c in zip(pos, col):
+        a.glColor4f(*map(float, c))
+        a.glVertex3f(*map(float, p))
+    a.glEnd()
+    b = F.base("arr", 128, 96, persp=False)
+    b.glEnable(G.GL_DEPTH_TEST)
+    b.glEnableClientState(G.GL_VERTEX_ARRAY)
+    b.glEnableClientState(G.GL_COLOR_ARRAY)
+    b.glVertexPointer(3, G.GL_FLOAT, 0, pos)
+    b.glColorPointer(4, G.GL_FLOAT, 0, col)
+    b.glDrawArrays(G.GL_TRIANGLES, 0, 300)
+    ra, rb = render(gpu, a), render(gpu, b)
+    harness.assert_parity(harness.compare(ra, rb), color_tol=0, name="immediate-vs-arrays")
+
+
+def test_many_draws_and_passes(gpu, oracle):
+    """Hundreds of small draws, interleaved clears (new passes) and buffer updates between draws."""
+    rng = np.random.default_rng(10)
+    s = F.base("many", 96, 64)
+    s.glEnable(G.GL_DEPTH_TEST)
+    s.glEnable(G.GL_BLEND)
+    s.glBlendFunc(G.GL_SRC_ALPHA, G.GL_ONE_MINUS_SRC_ALPHA)
+    vb = rng.uniform(-2, 2, (30, 3)).astype(np.float32)
+    vb[:, 2] = rng.uniform(-6, -2, 30)
+    s.glGenBuffers(1, np.zeros(1, np.uint32))
+    s.glBindBuffer(G.GL_ARRAY_BUFFER, 1)
+    s.glBufferData(G.GL_ARRAY_BUFFER, vb.nbytes, vb, G.GL_DYNAMIC_DRAW)
+    s.glEnableClientState(G.GL_VERTEX_ARRAY)
+    s.glVertexPointer(3, G.GL_FLOAT, 0, 0)
+    for i in range(120):
+        s.glColor4f(*map(float, rng.uniform(0, 1, 4)))
+        s.glDrawArrays(G.GL_TRIANGLES, 3 * (i % 10), 3)
+        if i % 17 == 5:
+            upd = np.ascontiguousarray(rng.uniform(-2, 2, 3).astype(np.float32))
+            s.glBufferSubData(G.GL_ARRAY_BUFFER, 12 * int(rng.integers(0, 30)), 12, upd)
+        if i % 40 == 39:
+            s.glEnable(G.GL_SCISSOR_TEST)
+            s.glScissor(int(rng.integers(0, 40)), int(rng.integers(0, 30)), 40, 30)
+            s.glClear(G.GL_DEPTH_BUFFER_BIT | G.GL_COLOR_BUFFER_BIT)
+            s.glDisable(G.GL_SCISSOR_TEST)
+    check(gpu, oracle, s)
+
+
+def test_readpixels(gpu, oracle):
+    scene = F.SCENES["blend"][0]()
+    outs = []
+    for lib in (oracle, gpu):
+        ctx = lib.context(scene.width, scene.height)
+        scene.play(ctx)
+        buf = np.zeros((50, 70, 4), np.uint8)
+        ctx.glReadPixels(-5, 30, 70, 50, G.GL_RGBA, G.GL_UNSIGNED_BYTE, buf)
+        outs.append(buf.copy())
+        ctx.destroy()
+    d = np.abs(outs[0].astype(int) - outs[1].astype(int))
+    assert d.max() <= 1
+
+
+@pytest.mark.parametrize("name", LINE_SCENES)
+def test_points_and_lines_are_reported(gpu, name):
+    """Points, lines and glPolygonMode POINT/LINE have no kernel yet: the draw is refused
+    with GL_INVALID_OPERATION instead of rendering something different."""
+    scene = F.SCENES[name][0]()
+    c, d, s, err = render(gpu, scene)
+    assert err == G.GL_INVALID_OPERATION

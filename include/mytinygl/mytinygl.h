@@ -46,6 +46,22 @@ int mtgl_get_timings(GLState *ctx, mtgl_timings *out);
 /* cudaStream_t of ctx, for callers that order their own GPU work with the renderer's. */
 void *mtgl_cuda_stream(GLState *ctx);
 
+/* Submit ctx's queued rendering without allocating any memory. No counterpart in the
+ * reference, which renders synchronously and allocates only host memory.
+ *
+ * For callers that cannot let the renderer call cudaMalloc/cudaFree while they render:
+ * real-time threads that cannot take the implied device-wide synchronisation, serving
+ * processes that keep all device memory under their own budget, hosts whose CUDA
+ * allocator belongs to another runtime. The queued pass runs exactly as on the normal
+ * path, but its scratch (vertices, triangle records, tile lists, sort and scan temporaries)
+ * comes from one static 64 MiB device array that every GPU loading the library holds.
+ * Returns 0, or MTGL_ERR_OVERFLOW when the pass needs more scratch than that or more
+ * staging than ctx already holds; the pass then stays queued and renders at the next
+ * mtgl_finish. All calls share the array: calls whose GPU work overlaps (contexts on
+ * different threads) race and must be serialised. The first call on a device looks up
+ * the array's address; make it before any stream capture. */
+int mtgl_flush_noalloc(GLState *ctx);
+
 #ifdef __cplusplus
 }
 #endif

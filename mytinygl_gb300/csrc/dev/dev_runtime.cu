@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "dev_kernels.h"
+#include "mytinygl/mytinygl.h"
 
 using namespace mtgl;
 
@@ -871,3 +872,279 @@ int mtgl_dev_reset_stats(mtgl_dev *d)
 }
 
 }  // extern "C"
+
+// ============================================================================================
+// Allocation-free flush.
+//
+// Some callers cannot let this library allocate device memory while they render: a
+// real-time render thread cannot afford the device-wide synchronisation cudaMalloc and
+// cudaFree imply; a serving process may keep every byte of device memory under its own
+// budget; code that owns the CUDA allocator (another runtime's memory pool) may forbid
+// foreign allocations. mtgl_flush_noalloc gives them the same pass pipeline as
+// mtgl_dev_flush with every per-pass scratch buffer (post-transform vertices, triangle
+// records, tile pairs, radix histograms, scan temporaries, tile counts) carved from one
+// file-scope device array of kNoAllocScratchBytes instead of from cudaMallocAsync.
+//
+// Limits: a pass whose scratch does not fit is refused with MTGL_ERR_OVERFLOW before
+// anything is drawn, and stays queued (mtgl_finish or mtgl_dev_flush can still render
+// it). The pass's tables must fit the staging areas the context already holds. Every
+// call, from every context on the device, shares the one array and overwrites what the
+// previous call left; calls whose work overlaps on the GPU (two contexts on different
+// streams) race, so callers serialise them. The array's device address is looked up
+// once per device, on the first call with that device current; make that first call
+// before any stream capture.
+// ============================================================================================
+#include <mutex>
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;  // 64 MiB held by every GPU that loads the library
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+uint8_t *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// set-up, once per device with that device current: host code needs the array's device address
+int noalloc_scratch(int device, uint8_t **out)
+{
+    if (device < 0 || device >= kNoAllocMaxDevices) {
+        snprintf(g_err, sizeof(g_err), "mtgl_flush_noalloc: device %d out of range", device);
+        return MTGL_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return fail_cuda("cudaGetSymbolAddress(g_noalloc_scratch)", e);
+        g_noalloc_addr[device] = static_cast<uint8_t *>(p);
+    }
+    *out = g_noalloc_addr[device];
+    return MTGL_OK;
+}
+
+// bump allocator over the static array (256-byte aligned pieces)
+struct Carve {
+    uint8_t *base;
+    size_t used, cap;
+    template <class T>
+    T *take(size_t n)
+    {
+        size_t at = (used + 255) & ~(size_t)255;
+        size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        if (at + bytes > cap) return nullptr;
+        used = at + bytes;
+        return reinterpret_cast<T *>(base + at);
+    }
+};
+
+int noalloc_overflow(const char *what, size_t need)
+{
+    snprintf(g_err, sizeof(g_err),
+             "mtgl_flush_noalloc: the pass needs more than the %zu-byte static scratch (%s, %zu bytes); "
+             "the pass stays queued",
+             kNoAllocScratchBytes, what, need);
+    return MTGL_ERR_OVERFLOW;
+}
+
+int flush_pass_noalloc(mtgl_dev *d)
+{
+    if (d->draws.empty()) return run_clears_only(d);  // clears launch kernels only
+    uint8_t *scratch = nullptr;
+    int st = noalloc_scratch(d->device, &scratch);
+    if (st) return st;
+    const size_t ndraws = d->draws.size();
+    const size_t hused0 = d->hused;
+
+    // tables into the existing staging area, without growing it
+    size_t at = hused0;
+    auto place = [&](size_t bytes) {
+        size_t off = align16(at);
+        at = off + bytes;
+        return (int64_t)off;
+    };
+    const int64_t off_draws = place(ndraws * sizeof(DevDraw));
+    const int64_t off_vbase = place(ndraws * sizeof(uint32_t));
+    const int64_t off_tbase = place(ndraws * sizeof(uint32_t));
+    const int64_t off_vs = place(d->vstates.size() * sizeof(mtgl_vertex_state));
+    const int64_t off_rs = place(d->rasters.size() * sizeof(DevRaster));
+    const int64_t off_clears = place(std::max<size_t>(1, d->clears.size()) * sizeof(ClearOp));
+    if (at > d->hcap || at > d->dcap) {
+        snprintf(g_err, sizeof(g_err),
+                 "mtgl_flush_noalloc: the pass's tables (%zu bytes) exceed the context's staging areas; "
+                 "the pass stays queued",
+                 at);
+        return MTGL_ERR_OVERFLOW;
+    }
+    if ((st = stage_begin(d))) return st;
+
+    const uint32_t slots = (uint32_t)d->slots, tris = (uint32_t)d->tris;
+    const bool eye = d->pass_needs_eye;
+    const uint32_t ntiles = (uint32_t)(d->dims.tiles_x * d->dims.tiles_y);
+    Carve cv{scratch, 0, kNoAllocScratchBytes};
+    PostVertex *verts = cv.take<PostVertex>(slots);
+    PostEye *eyes = eye ? cv.take<PostEye>(slots) : nullptr;
+    uint32_t *tri_counts = cv.take<uint32_t>(tris);
+    uint32_t *tri_offsets = cv.take<uint32_t>(tris);
+    uint32_t *tile_count = cv.take<uint32_t>(ntiles + 1);
+    uint32_t *tile_start = cv.take<uint32_t>(ntiles + 1);
+    uint32_t *scan_temp = cv.take<uint32_t>(scan_temp_words(std::max<uint32_t>(std::max(tris, ntiles), 1)));
+    if (!verts || (eye && !eyes) || !tri_counts || !tri_offsets || !tile_count || !tile_start || !scan_temp)
+        return noalloc_overflow("vertices and triangle counts", cv.used);
+
+    uint8_t *ds = d->dstage;
+    DevDraw *hd = reinterpret_cast<DevDraw *>(d->hstage + off_draws);
+    uint32_t *hvb = reinterpret_cast<uint32_t *>(d->hstage + off_vbase);
+    uint32_t *htb = reinterpret_cast<uint32_t *>(d->hstage + off_tbase);
+    for (size_t i = 0; i < ndraws; i++) {
+        PendingDraw &p = d->draws[i];
+        DevDraw dd = p.d;
+        if (p.off_pos >= 0) dd.pos.ptr = ds + p.off_pos;
+        if (p.off_color >= 0) dd.color.ptr = ds + p.off_color;
+        if (p.off_tex >= 0) dd.tex.ptr = ds + p.off_tex;
+        if (p.off_normal >= 0) dd.normal.ptr = ds + p.off_normal;
+        if (p.off_idx >= 0) dd.indices = ds + p.off_idx;
+        if (p.off_vsid >= 0) dd.vs_ids = reinterpret_cast<const uint32_t *>(ds + p.off_vsid);
+        hd[i] = dd;
+        hvb[i] = dd.vslot_base;
+        htb[i] = dd.tri_base;
+    }
+    if (!d->vstates.empty())
+        memcpy(d->hstage + off_vs, d->vstates.data(), d->vstates.size() * sizeof(mtgl_vertex_state));
+    memcpy(d->hstage + off_rs, d->rasters.data(), d->rasters.size() * sizeof(DevRaster));
+    if (!d->clears.empty()) memcpy(d->hstage + off_clears, d->clears.data(), d->clears.size() * sizeof(ClearOp));
+    CK(cudaMemcpyAsync(d->dstage, d->hstage, at, cudaMemcpyHostToDevice, d->stream));
+
+    GeomArgs ga;
+    memset(&ga, 0, sizeof(ga));
+    ga.draws = reinterpret_cast<const DevDraw *>(ds + off_draws);
+    ga.draw_vslot_base = reinterpret_cast<const uint32_t *>(ds + off_vbase);
+    ga.draw_tri_base = reinterpret_cast<const uint32_t *>(ds + off_tbase);
+    ga.ndraws = (int32_t)ndraws;
+    ga.vstates = reinterpret_cast<const mtgl_vertex_state *>(ds + off_vs);
+    ga.rasters = reinterpret_cast<const DevRaster *>(ds + off_rs);
+    ga.verts = verts;
+    ga.eyes = eyes;
+    ga.total_slots = slots;
+    ga.total_tris = tris;
+    ga.dims = d->dims;
+    ga.tri_counts = tri_counts;
+    ga.tri_offsets = tri_offsets;
+    int launches = 0;
+    launches += launch_vertex(ga, d->stream);
+    launches += launch_setup_count(ga, d->stream);
+    launches += launch_scan(tri_counts, tri_offsets, tris, scan_temp, d->d_totals + 0, d->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(d->h_totals, d->d_totals, sizeof(uint32_t), cudaMemcpyDeviceToHost, d->stream));
+    CK(cudaStreamSynchronize(d->stream));
+    const uint32_t nrec = d->h_totals[0];
+
+    float *records = cv.take<float>((size_t)nrec * kRecWords);
+    float *eye_records = eye ? cv.take<float>((size_t)nrec * kEyeWords) : nullptr;
+    uint32_t *rec_tiles = cv.take<uint32_t>(nrec);
+    if (!records || (eye && !eye_records) || !rec_tiles) {
+        d->hused = hused0;
+        return noalloc_overflow("triangle records", cv.used + (size_t)nrec * (kRecWords + kEyeWords + 1) * 4);
+    }
+    ga.records = records;
+    ga.eye_records = eye_records;
+    ga.records_cap = nrec;
+    launches += launch_setup_emit(ga, d->stream);
+
+    CK(cudaMemsetAsync(tile_count, 0, (ntiles + 1) * sizeof(uint32_t), d->stream));
+    BinArgs ba;
+    memset(&ba, 0, sizeof(ba));
+    ba.records = records;
+    ba.nrec = nrec;
+    ba.dims = d->dims;
+    ba.tile_count = tile_count;
+    ba.tile_start = tile_start;
+    ba.total_dev = d->d_totals + 1;
+    uint32_t npairs = 0;
+    if (nrec) {
+        uint32_t *rec_scan_temp = cv.take<uint32_t>(scan_temp_words(std::max(nrec, ntiles)));
+        if (!rec_scan_temp) {
+            d->hused = hused0;
+            return noalloc_overflow("record scan", cv.used);
+        }
+        ba.rec_tiles = rec_tiles;
+        ba.scan_temp = rec_scan_temp;
+        launches += launch_bin_count(ba, d->stream);
+        launches += launch_scan(rec_tiles, rec_tiles, nrec, rec_scan_temp, d->d_totals + 1, d->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(d->h_totals + 1, d->d_totals + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, d->stream));
+        CK(cudaStreamSynchronize(d->stream));
+        npairs = d->h_totals[1];
+        const size_t hist = radix_hist_words(npairs);
+        uint32_t *keys = cv.take<uint32_t>(npairs), *vals = cv.take<uint32_t>(npairs);
+        uint32_t *keys_alt = cv.take<uint32_t>(npairs), *vals_alt = cv.take<uint32_t>(npairs);
+        uint32_t *radix_hist = cv.take<uint32_t>(hist);
+        uint32_t *sort_scan_temp = cv.take<uint32_t>(
+            scan_temp_words(std::max<uint32_t>(std::max<uint32_t>((uint32_t)hist, nrec), ntiles)));
+        if (!keys || !vals || !keys_alt || !vals_alt || !radix_hist || !sort_scan_temp) {
+            d->hused = hused0;
+            return noalloc_overflow("tile pairs", cv.used + (size_t)npairs * 16);
+        }
+        ba.scan_temp = sort_scan_temp;
+        ba.keys = keys;
+        ba.vals = vals;
+        ba.keys_alt = keys_alt;
+        ba.vals_alt = vals_alt;
+        ba.radix_hist = radix_hist;
+        ba.npairs = npairs;
+        ba.pairs_cap = npairs;
+        launches += launch_bin_expand(ba, d->stream);
+        launches += launch_bin_sort(ba, d->stream);
+        scan_temp = sort_scan_temp;
+    }
+    launches += launch_scan(tile_count, tile_start, ntiles, scan_temp, d->d_totals + 2, d->stream);
+
+    TileArgs ta;
+    memset(&ta, 0, sizeof(ta));
+    ta.records = records;
+    ta.eye_records = eye_records;
+    ta.tile_vals = nrec ? ba.vals : nullptr;
+    ta.tile_start = tile_start;
+    ta.tile_count = tile_count;
+    ta.rasters = ga.rasters;
+    ta.nrasters = (uint32_t)d->rasters.size();
+    ta.clears = reinterpret_cast<const ClearOp *>(ds + off_clears);
+    ta.nclears = (int32_t)d->clears.size();
+    ta.dims = d->dims;
+    ta.color = d->color;
+    ta.depth = d->depth;
+    ta.stencil = d->stencil;
+    ta.fragments = d->d_frags;
+    launches += launch_tile(ta, d->stream);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(d->stage_done, d->stream));
+    d->stage_inflight = true;
+
+    d->stats.passes++;
+    d->stats.input_triangles += tris;
+    d->stats.setup_triangles += nrec;
+    d->stats.bin_entries += npairs;
+    d->stats.kernel_launches += (uint64_t)launches;
+    d->draws.clear();
+    d->clears.clear();
+    d->vstates.clear();
+    d->rasters.clear();
+    d->raster_src.clear();
+    d->pass_needs_eye = false;
+    d->slots = d->tris = 0;
+    d->hused = 0;
+    return MTGL_OK;
+}
+
+}  // namespace
+
+extern "C" mtgl_dev *fe_context_device(GLState *ctx);
+
+extern "C" int mtgl_flush_noalloc(GLState *ctx)
+{
+    mtgl_dev *d = ctx ? fe_context_device(ctx) : nullptr;
+    if (!d) return MTGL_ERR_INVALID;
+    CK(cudaSetDevice(d->device));
+    return flush_pass_noalloc(d);
+}

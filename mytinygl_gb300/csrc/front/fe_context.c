@@ -181,6 +181,9 @@ int mtgl_set_profiling(GLState *c, int enable) { return c ? mtgl_dev_profile(c->
 int mtgl_get_timings(GLState *c, mtgl_timings *out) { return c ? mtgl_dev_timings(c->dev, out) : MTGL_ERR_INVALID; }
 void *mtgl_cuda_stream(GLState *c) { return c ? mtgl_dev_stream(c->dev) : NULL; }
 
+/* the back end of a context, for back-end entry points that take a GLState (not exported) */
+mtgl_dev *fe_context_device(GLState *c) { return c ? c->dev : NULL; }
+
 /* ---- capabilities (gl_api.c:351-407) ---- */
 static uint32_t cap_flag(GLenum cap)
 {

@@ -27,6 +27,7 @@
 
 #include "GL/gl.h"
 #include "mytinygl/mtgl_dev.h"
+#include "mytinygl/mytinygl.h"
 
 /* ------------------------------------------------------------------ basics */
 
@@ -1377,4 +1378,10 @@ void *mtgl_dev_stream(mtgl_dev *d)
 {
     (void)d;
     return NULL;
+}
+
+/* The CPU oracle renders every packet as it arrives; nothing is ever queued. */
+int mtgl_flush_noalloc(GLState *ctx)
+{
+    return ctx ? MTGL_OK : MTGL_ERR_INVALID;
 }

@@ -52,7 +52,7 @@ WORKLOADS = {
     "sphere": dict(builder=W.sphere_scene, full_tris=1984, name="sphere_lit_800x600_1984",
                    desc="800x600 UV sphere (1,984 triangles), directional light, GL_LESS, back-face culling"),
 }
-REC_BYTES = 192  # triangle record written by the setup kernel, read by the tile kernel
+REC_BYTES = 224  # triangle record written by the setup kernel, read by the tile kernel
 
 
 class Stats(ctypes.Structure):
@@ -77,6 +77,25 @@ def bind_extras(lib):
     L.mtgl_get_timings.restype = ctypes.c_int
     L.mtgl_cuda_stream.argtypes = [ctypes.c_void_p]
     L.mtgl_cuda_stream.restype = ctypes.c_void_p
+    L.mtgl_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    L.mtgl_set_option.restype = ctypes.c_int
+
+
+MTGL_OPT_DEPTH_REJECTION = 1
+
+
+def covered_fragments(lib, scene, fs):
+    """Covered fragments of one frame (the F the reference runs through its per-pixel
+    pipeline), counted in an untimed frame with the tile kernel's depth rejection off."""
+    ctx = lib.context(scene.width, scene.height)
+    lib.lib.mtgl_set_option(ctx.handle, MTGL_OPT_DEPTH_REJECTION, 0)
+    scene.play(ctx, 0, fs)
+    ctx.glFinish()
+    lib.lib.mtgl_reset_stats(ctx.handle)
+    scene.play(ctx, fs)
+    frags = get_stats(ctx)["fragments"]
+    ctx.destroy()
+    return frags
 
 
 def get_stats(ctx):
@@ -236,8 +255,9 @@ def run_ours(args, spec):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     fps = world * args.steps / (total_ms / 1e3)
-    frags_per_frame = st["fragments"] / args.steps
+    tested_per_frame = st["fragments"] / args.steps
     ctx.destroy()
+    frags_per_frame = covered_fragments(lib, scene, fs)
 
     # ---- roofline of K4 (tile raster/ROP)
     peak, peak_src = measured_peaks()
@@ -293,6 +313,7 @@ def run_ours(args, spec):
                    "parallelism": f"replicas x{world}"},
         "fragments_per_s": round(frags_per_frame * fps, 1),
         "fragments_per_frame": int(frags_per_frame),
+        "depth_tested_fragments_per_frame": int(tested_per_frame),
         "triangles_per_s": round(st["input_triangles"] / args.steps * fps, 1),
         "phase_ms": {"vertex": round(tm.vertex_ms / max(1, tm.passes), 4),
                      "setup": round(tm.setup_ms / max(1, tm.passes), 4),

@@ -194,6 +194,13 @@ int mtgl_dev_timings(mtgl_dev *d, mtgl_timings *out);
 /* The cudaStream_t every operation of this context runs on (NULL for a CPU back end). */
 void *mtgl_dev_stream(mtgl_dev *d);
 
+/* Per-context options. MTGL_OPT_DEPTH_REJECTION (default 1): the tile kernel skips, per
+ * warp, triangles none of whose fragments can pass GL_LESS/GL_LEQUAL/GL_NEVER while the
+ * stencil test is off. Rendering is identical either way; with it off every covered
+ * fragment is counted in mtgl_stats.fragments. Applies to draws queued afterwards. */
+#define MTGL_OPT_DEPTH_REJECTION 1
+int mtgl_dev_set_option(mtgl_dev *d, int option, int value);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,8 @@ int mtgl_set_profiling(GLState *ctx, int enable);
 int mtgl_get_timings(GLState *ctx, mtgl_timings *out);
 /* cudaStream_t of ctx, for callers that order their own GPU work with the renderer's. */
 void *mtgl_cuda_stream(GLState *ctx);
+/* Back-end option of ctx (MTGL_OPT_* in mtgl_dev.h). */
+int mtgl_set_option(GLState *ctx, int option, int value);
 
 /* Submit ctx's queued rendering without allocating any memory. No counterpart in the
  * reference, which renders synchronously and allocates only host memory.

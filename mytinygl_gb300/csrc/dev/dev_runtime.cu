@@ -101,6 +101,7 @@ struct mtgl_dev {
     std::vector<cudaEvent_t> ev_pool;
     std::vector<cudaEvent_t> ev_pending;
     mtgl_timings timings{};
+    bool depth_rejection = true;
 };
 
 namespace {
@@ -200,6 +201,7 @@ uint32_t push_raster(mtgl_dev *d, const mtgl_raster_state *rs)
     }
     R.default_depth_range = (rs->depth_near == 0.0 && rs->depth_far == 1.0) ? 1 : 0;
     R.needs_eye = (rs->lighting && (rs->shade_model == GL_PHONG || rs->lit.two_side)) ? 1 : 0;
+    R.depth_rejection = d->depth_rejection ? 1 : 0;
     if (R.needs_eye) d->pass_needs_eye = true;
     d->raster_src.push_back(*rs);
     d->rasters.push_back(R);
@@ -859,6 +861,17 @@ int mtgl_dev_timings(mtgl_dev *d, mtgl_timings *out)
 }
 
 void *mtgl_dev_stream(mtgl_dev *d) { return d ? (void *)d->stream : nullptr; }
+
+int mtgl_dev_set_option(mtgl_dev *d, int option, int value)
+{
+    if (!d) return MTGL_ERR_INVALID;
+    if (option != MTGL_OPT_DEPTH_REJECTION) return MTGL_ERR_INVALID;
+    if (d->depth_rejection != (value != 0)) {
+        d->raster_src.clear();  // the next draw pushes a raster state carrying the new value
+        d->depth_rejection = value != 0;
+    }
+    return MTGL_OK;
+}
 
 int mtgl_dev_reset_stats(mtgl_dev *d)
 {

@@ -342,6 +342,39 @@ __device__ __forceinline__ void load_cv(const GeomArgs &A, uint32_t slot, bool e
     }
 }
 
+// Which depth rejection the tile kernel may apply to this triangle (ZCull). Only when the
+// stencil test is off (a depth-failed fragment then changes nothing), the depth function is
+// GL_LESS / GL_LEQUAL / GL_NEVER, the vertex depths are finite, and the triangle is small
+// enough that every edge-function value is an exact float integer (span_x * span_y < 2^23),
+// which the depth bound below relies on.
+__device__ __forceinline__ uint32_t depth_rejection(const DevRaster &R, float z0, float z1, float z2, float fx0,
+                                                   float fy0, float fx1, float fy1, float fx2, float fy2)
+{
+    const mtgl_raster_state &rs = R.rs;
+    if (!R.depth_rejection || !rs.depth_test || rs.stencil_test) return ZC_NONE;
+    if (rs.depth_func == GL_NEVER) return ZC_NEVER;
+    if (rs.depth_func != GL_LESS && rs.depth_func != GL_LEQUAL) return ZC_NONE;
+    if (!isfinite(z0) || !isfinite(z1) || !isfinite(z2)) return ZC_NONE;
+    const double sx = (double)fmaxf(fmaxf(fx0, fx1), fx2) - (double)fminf(fminf(fx0, fx1), fx2);
+    const double sy = (double)fmaxf(fmaxf(fy0, fy1), fy2) - (double)fminf(fminf(fy0, fy1), fy2);
+    if (!(sx * sy < 8388608.0)) return ZC_NONE;
+    return rs.depth_func == GL_LESS ? ZC_LESS : ZC_LEQUAL;
+}
+
+// Lower bound of every fragment depth of the triangle. For a covered pixel the tile kernel
+// computes b_i = e_i * inv_area >= 0 from exact edge values, so the weights e_i / area sum to
+// one and z = b0*z0 + b1*z1 + b2*z2 differs from that convex combination by at most
+// 5 * 2^-24 * max|z_i| (two roundings in b_i, three in the sum). The margin 2^-18 * max|z_i|
+// covers that and the rounding of the subtraction; the depth mapping is monotone.
+__device__ __forceinline__ float depth_lower_bound(const DevRaster &R, float z0, float z1, float z2)
+{
+    const float zmin = fminf(fminf(z0, z1), z2), zmax = fmaxf(fmaxf(z0, z1), z2);
+    const float zabs = fmaxf(fmaxf(fabsf(z0), fabsf(z1)), fabsf(z2));
+    const float margin = zabs * 0x1p-18f + 1e-37f;
+    const float dlo = map_depth(R, zmin - margin), dhi = map_depth(R, zmax + margin);
+    return fminf(dlo, dhi);
+}
+
 // Per fan triangle: the setup half of rasterize_triangle_smooth. Returns true when the
 // triangle produces a record; writes it when `rec` is non-null.
 __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raster_id, const FrameDims &dims, const CV &a,
@@ -400,19 +433,25 @@ __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raste
             }
         }
     }
+    const uint32_t zc = depth_rejection(R, a.clip.z, b.clip.z, c.clip.z, fx0, fy0, fx1, fy1, fx2, fy2);
+    const float dmin = zc == ZC_LESS || zc == ZC_LEQUAL ? depth_lower_bound(R, a.clip.z, b.clip.z, c.clip.z) : 0.0f;
     float4 *r4 = reinterpret_cast<float4 *>(rec);
     r4[0] = make_float4(fx0, fy0, fx1, fy1);
     r4[1] = make_float4(fx2, fy2, __int_as_float(minX), __int_as_float(minY));
     r4[2] = make_float4(__int_as_float(maxX), __int_as_float(maxY), area, inv_area);
-    r4[3] = make_float4(a.clip.z, b.clip.z, c.clip.z, a.clip.w);
-    r4[4] = make_float4(b.clip.w, c.clip.w, a.col.x, a.col.y);
-    r4[5] = make_float4(a.col.z, a.col.w, b.col.x, b.col.y);
-    r4[6] = make_float4(b.col.z, b.col.w, c.col.x, c.col.y);
-    r4[7] = make_float4(c.col.z, c.col.w, a.uv.x, a.uv.y);
-    r4[8] = make_float4(b.uv.x, b.uv.y, c.uv.x, c.uv.y);
-    r4[9] = make_float4(a.uv.x * a.clip.w, a.uv.y * a.clip.w, b.uv.x * b.clip.w, b.uv.y * b.clip.w);
-    r4[10] = make_float4(c.uv.x * c.clip.w, c.uv.y * c.clip.w, a.ez, b.ez);
-    r4[11] = make_float4(c.ez, lod, __uint_as_float(raster_id), __uint_as_float(back ? 1u : 0u));
+    r4[3] = make_float4(a.clip.z, b.clip.z, c.clip.z, dmin);
+    r4[4] = make_float4(a.clip.w, b.clip.w, c.clip.w, lod);
+    r4[5] = make_float4(a.col.x, a.col.y, a.col.z, a.col.w);
+    r4[6] = make_float4(b.col.x, b.col.y, b.col.z, b.col.w);
+    r4[7] = make_float4(c.col.x, c.col.y, c.col.z, c.col.w);
+    r4[8] = make_float4(a.uv.x, a.uv.y, b.uv.x, b.uv.y);
+    r4[9] = make_float4(c.uv.x, c.uv.y, a.uv.x * a.clip.w, a.uv.y * a.clip.w);
+    r4[10] = make_float4(b.uv.x * b.clip.w, b.uv.y * b.clip.w, c.uv.x * c.clip.w, c.uv.y * c.clip.w);
+    r4[11] = make_float4(a.ez, b.ez, c.ez, __uint_as_float(raster_id));
+    // edge_function(a, b, p) = (px - ax) * (by - ay) - (py - ay) * (bx - ax): the per-edge
+    // differences are the same floats whether formed per pixel or once here
+    r4[12] = make_float4(__uint_as_float((back ? 1u : 0u) | (zc << 1)), fy2 - fy1, fx2 - fx1, fy0 - fy2);
+    r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, 0.0f);
     if (eyerec) {
         float4 *e4 = reinterpret_cast<float4 *>(eyerec);
         e4[0] = make_float4(a.ep.x, a.ep.y, a.ep.z, a.en.x);

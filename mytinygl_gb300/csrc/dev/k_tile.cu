@@ -22,6 +22,127 @@ __device__ __forceinline__ bool covers_tile(const ClearOp &c, uint32_t bit, int 
     return (c.mask & bit) && c.x0 <= x0 && c.y0 <= y0 && c.x1 >= x1 && c.y1 >= y1;
 }
 
+// Float order as signed-int order (negative floats reversed), so a warp max is one REDUX.
+__device__ __forceinline__ int ordered_key(float f)
+{
+    const int b = __float_as_int(f);
+    return b ^ ((b >> 31) & 0x7FFFFFFF);
+}
+__device__ __forceinline__ float ordered_float(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7FFFFFFF)); }
+
+// Largest stored depth over the warp's pixels inside the framebuffer.
+__device__ __forceinline__ float warp_max_depth(float dep, bool in_fb)
+{
+    return ordered_float(__reduce_max_sync(0xffffffffu, in_fb ? ordered_key(dep) : INT32_MIN));
+}
+
+// One fragment of rasterize_triangle_smooth's pixel loop (raster.c:534-722) for this
+// thread's pixel. Returns true when it wrote the depth buffer.
+__device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, const float *e, bool have_eye, int px,
+                                            int py, float fpx, float fpy, uint32_t &col, float &dep, uint32_t &st,
+                                            uint32_t &frags)
+{
+    if (px < __float_as_int(r[R_MINX]) || px > __float_as_int(r[R_MAXX]) || py < __float_as_int(r[R_MINY]) ||
+        py > __float_as_int(r[R_MAXY]))
+        return false;
+    // edge_function at the integer pixel position (raster.c:299-302, 534-536)
+    const float e0 = (fpx - r[R_X1]) * r[R_EA0] - (fpy - r[R_Y1]) * r[R_EB0];
+    const float e1 = (fpx - r[R_X2]) * r[R_EA1] - (fpy - r[R_Y2]) * r[R_EB1];
+    const float e2 = (fpx - r[R_X0]) * r[R_EA2] - (fpy - r[R_Y0]) * r[R_EB2];
+    const float area = r[R_AREA];
+    if (!((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) || (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0))) return false;
+    frags++;
+    const float inv_area = r[R_INV_AREA];
+    const float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
+    const DevRaster &R = A.rasters[min(__float_as_uint(r[R_RASTER]), A.nrasters - 1)];
+    const mtgl_raster_state &rs = R.rs;
+    const float z = b0 * r[R_Z0] + b1 * r[R_Z1] + b2 * r[R_Z2];
+    const float depth = map_depth(R, z);
+
+    uint32_t sv = 0;
+    if (rs.stencil_test) {
+        sv = st;
+        if (!stencil_pass(rs.stencil_func, rs.stencil_ref, rs.stencil_mask, sv)) {
+            st = stencil_write(st, stencil_apply(rs.stencil_fail, sv, rs.stencil_ref), rs.stencil_writemask);
+            return false;
+        }
+    }
+    if (rs.depth_test && !cmp_pass(rs.depth_func, depth, dep)) {
+        if (rs.stencil_test)
+            st = stencil_write(st, stencil_apply(rs.stencil_zfail, sv, rs.stencil_ref), rs.stencil_writemask);
+        return false;
+    }
+    if (rs.stencil_test)
+        st = stencil_write(st, stencil_apply(rs.stencil_zpass, sv, rs.stencil_ref), rs.stencil_writemask);
+
+    float4 c;
+    if (rs.shade_model == GL_FLAT) {
+        c = make_float4(r[R_C2], r[R_C2 + 1], r[R_C2 + 2], r[R_C2 + 3]);
+    } else {
+        c = make_float4(r[R_C0] * b0 + r[R_C1] * b1 + r[R_C2] * b2,
+                        r[R_C0 + 1] * b0 + r[R_C1 + 1] * b1 + r[R_C2 + 1] * b2,
+                        r[R_C0 + 2] * b0 + r[R_C1 + 2] * b1 + r[R_C2 + 2] * b2,
+                        r[R_C0 + 3] * b0 + r[R_C1 + 3] * b1 + r[R_C2 + 3] * b2);
+    }
+    if (rs.lighting && have_eye) {
+        const bool back = (__float_as_uint(r[R_FLAGS]) & 1u) != 0;
+        const bool phong = rs.shade_model == GL_PHONG;
+        if (phong || (back && rs.lit.two_side)) {
+            float3 ep = make_float3(e[0] * b0 + e[6] * b1 + e[12] * b2, e[1] * b0 + e[7] * b1 + e[13] * b2,
+                                    e[2] * b0 + e[8] * b1 + e[14] * b2);
+            float3 en = make_float3(e[3] * b0 + e[9] * b1 + e[15] * b2, e[4] * b0 + e[10] * b1 + e[16] * b2,
+                                    e[5] * b0 + e[11] * b1 + e[17] * b2);
+            const mtgl_material *mat = &rs.lit.front;
+            if (back && rs.lit.two_side) {
+                en = make_float3(en.x * -1.0f, en.y * -1.0f, en.z * -1.0f);
+                mat = &rs.lit.back;
+            }
+            c = compute_lighting(rs.lit, ep, en, *mat);
+        }
+    }
+    if (R.tex) {
+        float u, v;
+        if (rs.perspective_hint != GL_FASTEST) {
+            const float uow = b0 * r[R_UW0] + b1 * r[R_UW1] + b2 * r[R_UW2];
+            const float vow = b0 * r[R_VW0] + b1 * r[R_VW1] + b2 * r[R_VW2];
+            const float oow = b0 * r[R_W0] + b1 * r[R_W1] + b2 * r[R_W2];
+            const float w = 1.0f / oow;
+            u = uow * w;
+            v = vow * w;
+        } else {
+            u = b0 * r[R_UV0] + b1 * r[R_UV1] + b2 * r[R_UV2];
+            v = b0 * r[R_UV0 + 1] + b1 * r[R_UV1 + 1] + b2 * r[R_UV2 + 1];
+        }
+        const float4 tc = unpack_rgba(sample_lod(R, u, v, r[R_LOD]));
+        // the alpha test applies to textured fragments only (raster.c:639-643)
+        if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) return false;
+        switch (rs.tex_env_mode) {
+        case GL_REPLACE: c = tc; break;
+        case GL_DECAL: c = lerp_rgb(c, tc, tc.w); break;
+        case GL_BLEND:
+            c = make_float4(c.x * (1.0f - tc.x) + rs.tex_env_color[0] * tc.x,
+                            c.y * (1.0f - tc.y) + rs.tex_env_color[1] * tc.y,
+                            c.z * (1.0f - tc.z) + rs.tex_env_color[2] * tc.z, c.w * tc.w);
+            break;
+        case GL_ADD: c = make_float4(c.x + tc.x, c.y + tc.y, c.z + tc.z, c.w * tc.w); break;
+        default: c = make_float4(c.x * tc.x, c.y * tc.y, c.z * tc.z, c.w * tc.w); break;
+        }
+    }
+    if (rs.fog) {
+        const float fc = b0 * r[R_EZ0] + b1 * r[R_EZ1] + b2 * r[R_EZ2];
+        c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, fc));
+    }
+    bool wrote = false;
+    if (rs.depth_test && rs.depth_mask) {
+        dep = depth;
+        wrote = true;
+    }
+    if (rs.blend) c = blend(rs, c, unpack_rgba(col));
+    c = clamp4(c);
+    col = masked_write(rs, col, c);
+    return wrote;
+}
+
 __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
 {
     __shared__ float4 s_rec[kChunk][kRecWords / 4];
@@ -68,6 +189,8 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
     const uint32_t start = A.tile_start[tile];
     uint32_t frags = 0;
     const bool have_eye = A.eye_records != nullptr;
+    // hierarchical z: the warp's largest stored depth, refreshed whenever the warp writes depth
+    float wzmax = warp_max_depth(dep, in_fb);
 
     for (uint32_t base = 0; base < count; base += kChunk) {
         const int n = (int)min((uint32_t)kChunk, count - base);
@@ -85,107 +208,18 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
             }
         }
         __syncthreads();
-        if (!in_fb) continue;
 
         for (int j = 0; j < n; j++) {
             const float *r = reinterpret_cast<const float *>(s_rec[j]);
-            if (px < __float_as_int(r[R_MINX]) || px > __float_as_int(r[R_MAXX]) || py < __float_as_int(r[R_MINY]) ||
-                py > __float_as_int(r[R_MAXY]))
-                continue;
-            const float x0 = r[R_X0], y0 = r[R_Y0], x1 = r[R_X1], y1 = r[R_Y1], x2 = r[R_X2], y2 = r[R_Y2];
-            // edge_function at the integer pixel position (raster.c:299-302, 534-536)
-            const float e0 = (fpx - x1) * (y2 - y1) - (fpy - y1) * (x2 - x1);
-            const float e1 = (fpx - x2) * (y0 - y2) - (fpy - y2) * (x0 - x2);
-            const float e2 = (fpx - x0) * (y1 - y0) - (fpy - y0) * (x1 - x0);
-            const float area = r[R_AREA];
-            if (!((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) || (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0)))
-                continue;
-            frags++;
-            const float inv_area = r[R_INV_AREA];
-            const float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
-            const DevRaster &R = A.rasters[min(__float_as_uint(r[R_RASTER]), A.nrasters - 1)];
-            const mtgl_raster_state &rs = R.rs;
-            const float z = b0 * r[R_Z0] + b1 * r[R_Z1] + b2 * r[R_Z2];
-            const float depth = map_depth(R, z);
-
-            uint32_t sv = 0;
-            if (rs.stencil_test) {
-                sv = st;
-                if (!stencil_pass(rs.stencil_func, rs.stencil_ref, rs.stencil_mask, sv)) {
-                    st = stencil_write(st, stencil_apply(rs.stencil_fail, sv, rs.stencil_ref), rs.stencil_writemask);
-                    continue;
-                }
+            // warp-uniform rejection: no fragment of this triangle can pass the depth test here
+            const uint32_t zc = (__float_as_uint(r[R_FLAGS]) >> 1) & 3u;
+            if (zc != ZC_NONE) {
+                const float dmin = r[R_DMIN];
+                if (zc == ZC_NEVER || dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)) continue;
             }
-            if (rs.depth_test && !cmp_pass(rs.depth_func, depth, dep)) {
-                if (rs.stencil_test)
-                    st = stencil_write(st, stencil_apply(rs.stencil_zfail, sv, rs.stencil_ref), rs.stencil_writemask);
-                continue;
-            }
-            if (rs.stencil_test)
-                st = stencil_write(st, stencil_apply(rs.stencil_zpass, sv, rs.stencil_ref), rs.stencil_writemask);
-
-            float4 c;
-            if (rs.shade_model == GL_FLAT) {
-                c = make_float4(r[R_C2], r[R_C2 + 1], r[R_C2 + 2], r[R_C2 + 3]);
-            } else {
-                c = make_float4(r[R_C0] * b0 + r[R_C1] * b1 + r[R_C2] * b2,
-                                r[R_C0 + 1] * b0 + r[R_C1 + 1] * b1 + r[R_C2 + 1] * b2,
-                                r[R_C0 + 2] * b0 + r[R_C1 + 2] * b1 + r[R_C2 + 2] * b2,
-                                r[R_C0 + 3] * b0 + r[R_C1 + 3] * b1 + r[R_C2 + 3] * b2);
-            }
-            if (rs.lighting && have_eye) {
-                const bool back = (__float_as_uint(r[R_FLAGS]) & 1u) != 0;
-                const bool phong = rs.shade_model == GL_PHONG;
-                if (phong || (back && rs.lit.two_side)) {
-                    const float *e = reinterpret_cast<const float *>(s_eye[j]);
-                    float3 ep = make_float3(e[0] * b0 + e[6] * b1 + e[12] * b2, e[1] * b0 + e[7] * b1 + e[13] * b2,
-                                            e[2] * b0 + e[8] * b1 + e[14] * b2);
-                    float3 en = make_float3(e[3] * b0 + e[9] * b1 + e[15] * b2, e[4] * b0 + e[10] * b1 + e[16] * b2,
-                                            e[5] * b0 + e[11] * b1 + e[17] * b2);
-                    const mtgl_material *mat = &rs.lit.front;
-                    if (back && rs.lit.two_side) {
-                        en = make_float3(en.x * -1.0f, en.y * -1.0f, en.z * -1.0f);
-                        mat = &rs.lit.back;
-                    }
-                    c = compute_lighting(rs.lit, ep, en, *mat);
-                }
-            }
-            if (R.tex) {
-                float u, v;
-                if (rs.perspective_hint != GL_FASTEST) {
-                    const float uow = b0 * r[R_UW0] + b1 * r[R_UW1] + b2 * r[R_UW2];
-                    const float vow = b0 * r[R_VW0] + b1 * r[R_VW1] + b2 * r[R_VW2];
-                    const float oow = b0 * r[R_W0] + b1 * r[R_W1] + b2 * r[R_W2];
-                    const float w = 1.0f / oow;
-                    u = uow * w;
-                    v = vow * w;
-                } else {
-                    u = b0 * r[R_UV0] + b1 * r[R_UV1] + b2 * r[R_UV2];
-                    v = b0 * r[R_UV0 + 1] + b1 * r[R_UV1 + 1] + b2 * r[R_UV2 + 1];
-                }
-                const float4 tc = unpack_rgba(sample_lod(R, u, v, r[R_LOD]));
-                // the alpha test applies to textured fragments only (raster.c:639-643)
-                if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) continue;
-                switch (rs.tex_env_mode) {
-                case GL_REPLACE: c = tc; break;
-                case GL_DECAL: c = lerp_rgb(c, tc, tc.w); break;
-                case GL_BLEND:
-                    c = make_float4(c.x * (1.0f - tc.x) + rs.tex_env_color[0] * tc.x,
-                                    c.y * (1.0f - tc.y) + rs.tex_env_color[1] * tc.y,
-                                    c.z * (1.0f - tc.z) + rs.tex_env_color[2] * tc.z, c.w * tc.w);
-                    break;
-                case GL_ADD: c = make_float4(c.x + tc.x, c.y + tc.y, c.z + tc.z, c.w * tc.w); break;
-                default: c = make_float4(c.x * tc.x, c.y * tc.y, c.z * tc.z, c.w * tc.w); break;
-                }
-            }
-            if (rs.fog) {
-                const float fc = b0 * r[R_EZ0] + b1 * r[R_EZ1] + b2 * r[R_EZ2];
-                c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, fc));
-            }
-            if (rs.depth_test && rs.depth_mask) dep = depth;
-            if (rs.blend) c = blend(rs, c, unpack_rgba(col));
-            c = clamp4(c);
-            col = masked_write(rs, col, c);
+            const bool wrote = shade_pixel(A, r, reinterpret_cast<const float *>(s_eye[j]), have_eye, px, py, fpx,
+                                           fpy, col, dep, st, frags);
+            if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
         }
     }
 

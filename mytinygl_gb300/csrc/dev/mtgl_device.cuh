@@ -19,7 +19,7 @@ namespace mtgl {
 
 constexpr int kTile = 16;            // tile edge in pixels (one CTA per tile)
 constexpr int kTileThreads = kTile * kTile;
-constexpr int kRecWords = 48;        // words per triangle record
+constexpr int kRecWords = 56;        // words per triangle record (224 bytes)
 constexpr int kEyeWords = 20;        // words per triangle eye-space record (per-fragment lighting)
 
 // Triangle record written by the setup kernel, read by the tile kernel (raster.c:451-529
@@ -29,15 +29,23 @@ enum RecField {
     R_MINX = 6, R_MINY, R_MAXX, R_MAXY,       // int32 bbox after viewport/scissor/framebuffer clamps
     R_AREA = 10, R_INV_AREA,
     R_Z0 = 12, R_Z1, R_Z2,
-    R_W0 = 15, R_W1, R_W2,                    // 1/w
-    R_C0 = 18, R_C1 = 22, R_C2 = 26,          // RGBA each
-    R_UV0 = 30, R_UV1 = 32, R_UV2 = 34,       // raw texcoords
-    R_UW0 = 36, R_VW0, R_UW1, R_VW1, R_UW2, R_VW2,
-    R_EZ0 = 42, R_EZ1, R_EZ2,
-    R_LOD = 45,
-    R_RASTER = 46,                            // uint32 raster-state index
-    R_FLAGS = 47                              // bit 0: back facing
+    R_DMIN = 15,                              // lower bound of every fragment depth (hierarchical z)
+    R_W0 = 16, R_W1, R_W2,                    // 1/w
+    R_LOD = 19,
+    R_C0 = 20, R_C1 = 24, R_C2 = 28,          // RGBA each
+    R_UV0 = 32, R_UV1 = 34, R_UV2 = 36,       // raw texcoords
+    R_UW0 = 38, R_VW0, R_UW1, R_VW1, R_UW2, R_VW2,
+    R_EZ0 = 44, R_EZ1, R_EZ2,
+    R_RASTER = 47,                            // uint32 raster-state index
+    R_FLAGS = 48,                             // bit 0 back facing; bits 1-2 depth rejection mode
+    R_EA0 = 49, R_EB0, R_EA1, R_EB1, R_EA2, R_EB2,  // per-edge (by-ay), (bx-ax) of edge_function
+    R_PAD = 55
 };
+
+// Depth rejection modes (R_FLAGS bits 1-2). A warp skips a triangle when no fragment of it
+// can pass the depth test and a failing fragment has no other effect (stencil test off):
+// GL_LESS: min fragment depth >= the warp's max stored depth; GL_LEQUAL: >; GL_NEVER: always.
+enum ZCull { ZC_NONE = 0, ZC_LESS = 1, ZC_LEQUAL = 2, ZC_NEVER = 3 };
 
 // Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).
 struct __align__(16) PostVertex {
@@ -86,6 +94,8 @@ struct DevRaster {
     int32_t tex_w, tex_h, mip_w, mip_h;
     int32_t default_depth_range;
     int32_t needs_eye;     // per-fragment lighting reads eye-space interpolants
+    int32_t depth_rejection;  // MTGL_OPT_DEPTH_REJECTION of the context at enqueue
+    int32_t pad_;
 };
 
 struct ClearOp {

@@ -180,6 +180,10 @@ int mtgl_reset_stats(GLState *c) { return c ? mtgl_dev_reset_stats(c->dev) : MTG
 int mtgl_set_profiling(GLState *c, int enable) { return c ? mtgl_dev_profile(c->dev, enable) : MTGL_ERR_INVALID; }
 int mtgl_get_timings(GLState *c, mtgl_timings *out) { return c ? mtgl_dev_timings(c->dev, out) : MTGL_ERR_INVALID; }
 void *mtgl_cuda_stream(GLState *c) { return c ? mtgl_dev_stream(c->dev) : NULL; }
+int mtgl_set_option(GLState *c, int option, int value)
+{
+    return c ? mtgl_dev_set_option(c->dev, option, value) : MTGL_ERR_INVALID;
+}
 
 /* the back end of a context, for back-end entry points that take a GLState (not exported) */
 mtgl_dev *fe_context_device(GLState *c) { return c ? c->dev : NULL; }

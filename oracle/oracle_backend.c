@@ -1385,3 +1385,10 @@ int mtgl_flush_noalloc(GLState *ctx)
 {
     return ctx ? MTGL_OK : MTGL_ERR_INVALID;
 }
+
+int mtgl_dev_set_option(mtgl_dev *d, int option, int value)
+{
+    (void)d;
+    (void)value;
+    return option == MTGL_OPT_DEPTH_REJECTION ? MTGL_OK : MTGL_ERR_INVALID;
+}

@@ -37,3 +37,4 @@ int mtgl_reset_stats(GLState *ctx) { (void)ctx; return 1; }
 int mtgl_set_profiling(GLState *ctx, int enable) { (void)ctx; (void)enable; return 1; }
 int mtgl_get_timings(GLState *ctx, void *out) { (void)ctx; (void)out; return 1; }
 void *mtgl_cuda_stream(GLState *ctx) { (void)ctx; return 0; }
+int mtgl_set_option(GLState *ctx, int option, int value) { (void)ctx; (void)option; (void)value; return 1; }

@@ -136,3 +136,23 @@ def test_points_and_lines_are_reported(gpu, name):
     scene = F.SCENES[name][0]()
     c, d, s, err = render(gpu, scene)
     assert err == G.GL_INVALID_OPERATION
+
+
+@pytest.mark.parametrize("which", ["textured", "zbuffer", "depth_range", "clip_big", "stencil", "mipmap_floor"])
+def test_depth_rejection_changes_nothing(gpu, which):
+    """Hierarchical-z rejection in the tile kernel only skips fragments that cannot pass the
+    depth test and have no other effect: images are identical with it on and off, and with
+    it off every covered fragment is counted."""
+    import ctypes
+
+    scene = W.textured_scene(480, 270, ntri=6000) if which == "textured" else F.SCENES[which][0]()
+    gpu.lib.mtgl_set_option.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    gpu.lib.mtgl_set_option.restype = ctypes.c_int
+    outs = []
+    for enabled in (1, 0):
+        ctx = gpu.context(scene.width, scene.height)
+        assert gpu.lib.mtgl_set_option(ctx.handle, 1, enabled) == 0
+        scene.play(ctx)
+        outs.append(ctx.read() + (ctx.glGetError(),))
+        ctx.destroy()
+    harness.assert_parity(harness.compare(outs[0], outs[1]), color_tol=0, name=f"{which} rejection on/off")

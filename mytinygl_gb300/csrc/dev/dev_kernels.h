@@ -74,6 +74,7 @@ struct TileArgs {
     uint32_t nrasters;
     const ClearOp *clears;
     int32_t nclears;
+    int32_t any_texture;         // some raster state of the pass samples a texture
     FrameDims dims;
     uint32_t *color;
     float *depth;

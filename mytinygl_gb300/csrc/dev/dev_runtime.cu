@@ -451,6 +451,8 @@ int flush_pass(mtgl_dev *d)
     ta.nrasters = (uint32_t)d->rasters.size();
     ta.clears = reinterpret_cast<const ClearOp *>(ds + off_clears);
     ta.nclears = (int32_t)d->clears.size();
+    ta.any_texture = 0;
+    for (const DevRaster &R : d->rasters) ta.any_texture |= R.tex != nullptr;
     ta.dims = d->dims;
     ta.color = d->color;
     ta.depth = d->depth;
@@ -1124,6 +1126,8 @@ int flush_pass_noalloc(mtgl_dev *d)
     ta.nrasters = (uint32_t)d->rasters.size();
     ta.clears = reinterpret_cast<const ClearOp *>(ds + off_clears);
     ta.nclears = (int32_t)d->clears.size();
+    ta.any_texture = 0;
+    for (const DevRaster &R : d->rasters) ta.any_texture |= R.tex != nullptr;
     ta.dims = d->dims;
     ta.color = d->color;
     ta.depth = d->depth;

@@ -15,7 +15,7 @@
 
 namespace mtgl {
 
-constexpr int kChunk = 32;  // records staged per step
+constexpr int kChunk = 32;  // records staged per step: one per lane for the overlap ballot
 
 __device__ __forceinline__ bool covers_tile(const ClearOp &c, uint32_t bit, int x0, int y0, int x1, int y1)
 {
@@ -37,7 +37,9 @@ __device__ __forceinline__ float warp_max_depth(float dep, bool in_fb)
 }
 
 // One fragment of rasterize_triangle_smooth's pixel loop (raster.c:534-722) for this
-// thread's pixel. Returns true when it wrote the depth buffer.
+// thread's pixel. Returns true when it wrote the depth buffer. TEX / EYE compile the
+// texturing and per-fragment lighting stages in only for passes that use them.
+template <bool TEX, bool EYE>
 __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, const float *e, bool have_eye, int px,
                                             int py, float fpx, float fpy, uint32_t &col, float &dep, uint32_t &st,
                                             uint32_t &frags)
@@ -84,7 +86,7 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, c
                         r[R_C0 + 2] * b0 + r[R_C1 + 2] * b1 + r[R_C2 + 2] * b2,
                         r[R_C0 + 3] * b0 + r[R_C1 + 3] * b1 + r[R_C2 + 3] * b2);
     }
-    if (rs.lighting && have_eye) {
+    if (EYE && rs.lighting && have_eye) {
         const bool back = (__float_as_uint(r[R_FLAGS]) & 1u) != 0;
         const bool phong = rs.shade_model == GL_PHONG;
         if (phong || (back && rs.lit.two_side)) {
@@ -100,7 +102,7 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, c
             c = compute_lighting(rs.lit, ep, en, *mat);
         }
     }
-    if (R.tex) {
+    if (TEX && R.tex) {
         float u, v;
         if (rs.perspective_hint != GL_FASTEST) {
             const float uow = b0 * r[R_UW0] + b1 * r[R_UW1] + b2 * r[R_UW2];
@@ -143,6 +145,7 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, c
     return wrote;
 }
 
+template <bool TEX, bool EYE>
 __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
 {
     __shared__ float4 s_rec[kChunk][kRecWords / 4];
@@ -188,7 +191,9 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
     const float fpx = (float)px, fpy = (float)py;
     const uint32_t start = A.tile_start[tile];
     uint32_t frags = 0;
-    const bool have_eye = A.eye_records != nullptr;
+    const bool have_eye = EYE && A.eye_records != nullptr;
+    // this warp's 8x4 pixel block: a staged record is visited only by the warps it overlaps
+    const int wx0 = tx * kTile + (warp & 1) * 8, wy0 = ty * kTile + (warp >> 1) * 4;
     // hierarchical z: the warp's largest stored depth, refreshed whenever the warp writes depth
     float wzmax = warp_max_depth(dep, in_fb);
 
@@ -209,7 +214,18 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
         }
         __syncthreads();
 
-        for (int j = 0; j < n; j++) {
+        // lane j tests staged record j's bbox against the warp's block; the set bits, taken
+        // lowest first, are this warp's records of the chunk in submission order
+        bool overlap = false;
+        if (lane < n) {
+            const float4 bb = s_rec[lane][1], bb2 = s_rec[lane][2];
+            overlap = !(__float_as_int(bb2.x) < wx0 || __float_as_int(bb.z) > wx0 + 7 ||
+                        __float_as_int(bb2.y) < wy0 || __float_as_int(bb.w) > wy0 + 3);
+        }
+        uint32_t todo = __ballot_sync(0xffffffffu, overlap);
+        while (todo) {
+            const int j = __ffs(todo) - 1;
+            todo &= todo - 1;
             const float *r = reinterpret_cast<const float *>(s_rec[j]);
             // warp-uniform rejection: no fragment of this triangle can pass the depth test here
             const uint32_t zc = (__float_as_uint(r[R_FLAGS]) >> 1) & 3u;
@@ -217,8 +233,8 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
                 const float dmin = r[R_DMIN];
                 if (zc == ZC_NEVER || dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)) continue;
             }
-            const bool wrote = shade_pixel(A, r, reinterpret_cast<const float *>(s_eye[j]), have_eye, px, py, fpx,
-                                           fpy, col, dep, st, frags);
+            const bool wrote = shade_pixel<TEX, EYE>(A, r, reinterpret_cast<const float *>(s_eye[j]), have_eye, px,
+                                                     py, fpx, fpy, col, dep, st, frags);
             if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
         }
     }
@@ -238,7 +254,11 @@ int launch_tile(const TileArgs &a, cudaStream_t s)
 {
     const int ntiles = a.dims.tiles_x * a.dims.tiles_y;
     if (ntiles == 0) return 0;
-    k_tile<<<ntiles, kTileThreads, 0, s>>>(a);
+    const bool eye = a.eye_records != nullptr;
+    if (a.any_texture && eye) k_tile<true, true><<<ntiles, kTileThreads, 0, s>>>(a);
+    else if (a.any_texture) k_tile<true, false><<<ntiles, kTileThreads, 0, s>>>(a);
+    else if (eye) k_tile<false, true><<<ntiles, kTileThreads, 0, s>>>(a);
+    else k_tile<false, false><<<ntiles, kTileThreads, 0, s>>>(a);
     return 1;
 }
 

@@ -450,7 +450,12 @@ __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raste
     r4[11] = make_float4(a.ez, b.ez, c.ez, __uint_as_float(raster_id));
     // edge_function(a, b, p) = (px - ax) * (by - ay) - (py - ay) * (bx - ax): the per-edge
     // differences are the same floats whether formed per pixel or once here
-    r4[12] = make_float4(__uint_as_float((back ? 1u : 0u) | (zc << 1)), fy2 - fy1, fx2 - fx1, fy0 - fy2);
+    const mtgl_raster_state &ds = R.rs;
+    const bool raises = ds.depth_test && ds.depth_mask &&
+                        (ds.depth_func == GL_GREATER || ds.depth_func == GL_GEQUAL || ds.depth_func == GL_NOTEQUAL ||
+                         ds.depth_func == GL_ALWAYS);
+    const uint32_t flags = (back ? 1u : 0u) | (zc << 1) | (raises ? kFlagRaisesDepth : 0u);
+    r4[12] = make_float4(__uint_as_float(flags), fy2 - fy1, fx2 - fx1, fy0 - fy2);
     r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, 0.0f);
     if (eyerec) {
         float4 *e4 = reinterpret_cast<float4 *>(eyerec);

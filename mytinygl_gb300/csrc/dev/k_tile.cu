@@ -214,15 +214,27 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
         }
         __syncthreads();
 
-        // lane j tests staged record j's bbox against the warp's block; the set bits, taken
-        // lowest first, are this warp's records of the chunk in submission order
-        bool overlap = false;
+        // Lane j tests staged record j against the warp: its bbox must meet the warp's block,
+        // and the depth rejection is tried with the warp's max depth as of now. That value is
+        // still an upper bound when record j is reached unless an earlier record of the chunk
+        // may raise depths, so rejection is only taken when none before j can. The set bits,
+        // lowest first, are this warp's records of the chunk in submission order.
+        bool take = false;
+        uint32_t raises = 0;
         if (lane < n) {
             const float4 bb = s_rec[lane][1], bb2 = s_rec[lane][2];
-            overlap = !(__float_as_int(bb2.x) < wx0 || __float_as_int(bb.z) > wx0 + 7 ||
-                        __float_as_int(bb2.y) < wy0 || __float_as_int(bb.w) > wy0 + 3);
+            take = !(__float_as_int(bb2.x) < wx0 || __float_as_int(bb.z) > wx0 + 7 || __float_as_int(bb2.y) < wy0 ||
+                     __float_as_int(bb.w) > wy0 + 3);
+            raises = __float_as_uint(reinterpret_cast<const float *>(s_rec[lane])[R_FLAGS]) & kFlagRaisesDepth;
         }
-        uint32_t todo = __ballot_sync(0xffffffffu, overlap);
+        const uint32_t raise_mask = __ballot_sync(0xffffffffu, raises != 0);
+        if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
+            const float *rl = reinterpret_cast<const float *>(s_rec[lane]);
+            const uint32_t zc = (__float_as_uint(rl[R_FLAGS]) >> 1) & 3u;
+            const float dmin = rl[R_DMIN];
+            if (zc == ZC_NEVER || (zc != ZC_NONE && (dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)))) take = false;
+        }
+        uint32_t todo = __ballot_sync(0xffffffffu, take);
         while (todo) {
             const int j = __ffs(todo) - 1;
             todo &= todo - 1;

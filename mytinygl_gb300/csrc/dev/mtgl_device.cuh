@@ -46,6 +46,9 @@ enum RecField {
 // can pass the depth test and a failing fragment has no other effect (stencil test off):
 // GL_LESS: min fragment depth >= the warp's max stored depth; GL_LEQUAL: >; GL_NEVER: always.
 enum ZCull { ZC_NONE = 0, ZC_LESS = 1, ZC_LEQUAL = 2, ZC_NEVER = 3 };
+// R_FLAGS bit 3: the triangle may raise stored depths (depth writes with GL_GREATER,
+// GL_GEQUAL, GL_NOTEQUAL or GL_ALWAYS); a warp's max depth taken before it is then no bound.
+constexpr uint32_t kFlagRaisesDepth = 8u;
 
 // Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).
 struct __align__(16) PostVertex {

@@ -58,11 +58,14 @@ class Scene:
             calls.append([name, enc])
         meta = {"name": self.name, "width": self.width, "height": self.height, "calls": calls}
         buf = io.BytesIO()
+        arr = io.BytesIO()
+        np.savez(arr, **arrays)
+        # fixed member dates keep the bytes a function of the script alone
         with zipfile.ZipFile(buf, "w", zipfile.ZIP_DEFLATED) as z:
-            z.writestr("scene.json", json.dumps(meta))
-            arr = io.BytesIO()
-            np.savez(arr, **arrays)
-            z.writestr("arrays.npz", arr.getvalue())
+            for member, data in (("scene.json", json.dumps(meta).encode()), ("arrays.npz", arr.getvalue())):
+                info = zipfile.ZipInfo(member, date_time=(1980, 1, 1, 0, 0, 0))
+                info.compress_type = zipfile.ZIP_DEFLATED
+                z.writestr(info, data)
         return buf.getvalue()
 
     @staticmethod

@@ -609,6 +609,19 @@ def sc_texture_matrix():
     return s
 
 
+def sc_depth_mix():
+    """Depth writes that raise stored depth (GL_ALWAYS, GL_GREATER, GL_NOTEQUAL) interleaved,
+    triangle by triangle, with GL_LESS / GL_LEQUAL draws over the same pixels."""
+    s = base("depth_mix", 64, 48)
+    rng = np.random.default_rng(36)
+    s.glEnable(G.GL_DEPTH_TEST)
+    funcs = (G.GL_LESS, G.GL_LEQUAL, G.GL_ALWAYS, G.GL_GREATER, G.GL_LESS, G.GL_NOTEQUAL, G.GL_GEQUAL)
+    for i in range(160):
+        s.glDepthFunc(funcs[int(rng.integers(0, len(funcs)))])
+        rand_tris(s, rng, 1, spread=1.5, z=(-8.0, -1.5))
+    return s
+
+
 SCENES = {
     "clip_big": (sc_clip_big, ()),
     "clip_near_far": (sc_clip_near_far, ()),
@@ -641,4 +654,5 @@ SCENES = {
     "draw_pixels": (sc_draw_pixels, ()),
     "phong_textured_fog": (sc_phong_textured_fog, ()),
     "texture_matrix": (sc_texture_matrix, ()),
+    "depth_mix": (sc_depth_mix, ()),
 }

@@ -35,6 +35,8 @@ def main():
     for name, scene in golden_scenes():
         c, d, s, err = render(ref, scene)
         bufs = harness.cleared_buffers(scene)
+        # a buffer the scene never clears holds the reference's uninitialised memory: store zeros
+        c, d, s = (x if bufs[k] else np.zeros_like(x) for x, k in ((c, "color"), (d, "depth"), (s, "stencil")))
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, scene=np.frombuffer(scene.to_bytes(), np.uint8), color=c, depth=d, stencil=s,
                             error=np.int64(err), defined_color=bufs["color"], defined_depth=bufs["depth"],

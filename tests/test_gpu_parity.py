@@ -138,7 +138,8 @@ def test_points_and_lines_are_reported(gpu, name):
     assert err == G.GL_INVALID_OPERATION
 
 
-@pytest.mark.parametrize("which", ["textured", "zbuffer", "depth_range", "clip_big", "stencil", "mipmap_floor"])
+@pytest.mark.parametrize("which", ["textured", "zbuffer", "depth_range", "clip_big", "stencil", "mipmap_floor",
+                                   "depth_mix"])
 def test_depth_rejection_changes_nothing(gpu, which):
     """Hierarchical-z rejection in the tile kernel only skips fragments that cannot pass the
     depth test and have no other effect: images are identical with it on and off, and with

@@ -52,7 +52,12 @@ WORKLOADS = {
     "sphere": dict(builder=W.sphere_scene, full_tris=1984, name="sphere_lit_800x600_1984",
                    desc="800x600 UV sphere (1,984 triangles), directional light, GL_LESS, back-face culling"),
 }
+WORKLOADS["batch"] = dict(builder=None, full_tris=None, name="uneven_batch_256_frames",
+                          desc=("256 independent frames, sides log-uniform 64-1024, triangles log-uniform "
+                                "100-200k, each a lit UV sphere or a clip-straddling textured frame (p=1/2) "
+                                "with its own modelview, lights and 256^2 mipmapped texture; seed 3"))
 REC_BYTES = 224  # triangle record written by the setup kernel, read by the tile kernel
+BATCH_FRAMES = 256
 
 
 class Stats(ctypes.Structure):
@@ -338,6 +343,230 @@ def run_ours(args, spec):
     return out if rank == 0 else None
 
 
+def tex_bytes_of(scene):
+    n = 0
+    for name, a in scene.cmds:
+        if name == "glTexImage2D":
+            w, h = int(a[3]), int(a[4])
+            n += 4 * (w * h + (w // 2) * (h // 2))
+    return n
+
+
+def setup_batch_frames(lib, scenes):
+    ctxs, streams = [], []
+    for sc in scenes:
+        c = lib.context(sc.width, sc.height)
+        k = W.frame_start(sc)
+        sc.play(c, 0, k)
+        ctxs.append(c)
+        streams.append(sc.stream(k))
+    for c in ctxs:
+        c.glFinish()
+    return ctxs, G.PreparedStreams(lib, ctxs, streams)
+
+
+def run_batch(args, spec):
+    """The uneven-batch workload: 256 frames of different sizes and loads per step.
+
+    value: frames/s of the batched path (one mtgl_batch_render of all frames per step,
+    replayed from its CUDA graph), CUDA events on the batch's stream around the submission,
+    L2 flushed before each step. batched_wall / plain_wall: the same frames on the host
+    clock through the batched path and through the plain per-frame path (glFinish on each
+    context), GL calls replayed natively (mtgl_play_many) in both."""
+    import torch
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import mytinygl_gb300 as M
+
+    M.build()
+    lib = M.library()
+    bind_extras(lib)
+    scenes = W.uneven_batch(BATCH_FRAMES)
+    ctxs, streams = setup_batch_frames(lib, scenes)
+    npix = sum(sc.width * sc.height for sc in scenes)
+    tris = sum(W.scene_triangles(sc) for sc in scenes)
+    batch = lib.batch()
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ext = torch.cuda.ExternalStream(batch.stream)
+    for _ in range(args.warmup):
+        streams.play()
+        batch.render(ctxs)
+        batch.wait()
+    batch.reset_stats()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            streams.play()  # host: each frame's GL calls queue its pass
+            with torch.cuda.stream(ext):
+                flush_buf.zero_()
+                starts[i].record(ext)
+            batch.render(ctxs)
+            ends[i].record(ext)
+        batch.wait()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    total_ms = sum(s_.elapsed_time(e) for s_, e in zip(starts, ends))
+    bst = batch.stats()
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    fps = world * args.steps * BATCH_FRAMES / (total_ms / 1e3)
+    batched_wall_fps = args.steps * BATCH_FRAMES / wall
+
+    # plain per-frame path, same frames, host clock
+    for c in ctxs:
+        c.glFinish()
+    torch.cuda.synchronize()
+    plain_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        for c, b in zip(ctxs, streams._bufs):
+            lib.lib.mtgl_play(c.handle, b, len(b))
+            c.glFinish()
+    plain_wall = time.perf_counter() - t0
+    plain_fps = plain_steps * BATCH_FRAMES / plain_wall
+
+    # per-phase device time from a profiled run without the graph (K4 roofline)
+    pbatch = lib.batch(use_graph=0)
+    streams.play()
+    pbatch.render(ctxs)
+    pbatch.wait()
+    pbatch.profile(True)
+    for _ in range(3):
+        streams.play()
+        pbatch.render(ctxs)
+    tm = pbatch.timings()
+    pst = pbatch.stats()
+    pbatch.destroy()
+    passes = max(1, tm["passes"])
+    k4_ms = tm["tile_ms"] / passes
+    rec = bst["setup_triangles"] / max(1, bst["batches"])
+    pairs = bst["bin_entries"] / max(1, bst["batches"])
+    tex = sum(tex_bytes_of(sc) for sc in scenes)
+    k4_bytes = npix * 9 + pairs * 4 + rec * REC_BYTES + tex
+    peak, peak_src = measured_peaks()
+    achieved = k4_bytes / (k4_ms / 1e3) / 1e9 if k4_ms > 0 else None
+
+    # fragments per batch with depth rejection off (untimed)
+    frags = 0
+    for c, sc in zip(ctxs, scenes):
+        frags += covered_fragments(lib, sc, W.frame_start(sc))
+
+    # e2e: client vertex arrays staged every step, every colour buffer read back
+    escenes = W.uneven_batch(BATCH_FRAMES, use_vbo=False)
+    ectxs, estreams = setup_batch_frames(lib, escenes)
+    hosts = [np.empty((sc.height, sc.width), np.uint32) for sc in escenes]
+    ebatch = lib.batch()
+    for _ in range(args.warmup):
+        estreams.play()
+        ebatch.render(ectxs)
+        ebatch.wait()
+    e_steps = max(1, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        estreams.play()
+        ebatch.render(ectxs)
+        for c, h in zip(ectxs, hosts):
+            lib.lib.mtgl_read_framebuffer(c.handle, h.ctypes.data, None, None)
+    e2e_s = time.perf_counter() - t0
+    ebatch.destroy()
+    h2d = sum(scene_bytes(sc, W.frame_start(sc)) for sc in escenes)
+    for c in ectxs:
+        c.destroy()
+    batch.destroy()
+    for c in ctxs:
+        c.destroy()
+
+    out = {
+        "metric": "frames/s",
+        "value": round(fps, 2),
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded; mytinygl_gb300/workloads.py uneven_batch)",
+        "config": {"workload": spec["name"], "description": spec["desc"], "frames_per_step": BATCH_FRAMES,
+                   "pixels_per_step": npix, "input_triangles_per_step": tris,
+                   "setup_triangles_per_step": int(rec), "bin_entries_per_step": int(pairs),
+                   "tile": bst["tile_size"], "persistent_ctas": bst["ctas"],
+                   "record_capacity": bst["record_capacity"], "pair_capacity": bst["pair_capacity"],
+                   "graph_replays": bst["graph_replays"], "graph_captures": bst["graph_captures"],
+                   "l2": "flushed before every timed step (256 MiB write on the batch stream)",
+                   "parallelism": f"replicas x{world}"},
+        "batched_wall_frames_per_s": round(batched_wall_fps, 2),
+        "plain_wall_frames_per_s": round(plain_fps, 2),
+        "batched_vs_plain_wall": round(batched_wall_fps / plain_fps, 3),
+        "fragments_per_s": round(frags * fps / BATCH_FRAMES, 1),
+        "fragments_per_step": int(frags),
+        "triangles_per_s": round(tris * fps / BATCH_FRAMES, 1),
+        "phase_ms": {"vertex": round(tm["vertex_ms"] / passes, 4), "setup": round(tm["setup_ms"] / passes, 4),
+                     "bin": round(tm["bin_ms"] / passes, 4), "tile": round(k4_ms, 4)},
+        "wall_ms_per_step": round(wall * 1e3 / args.steps, 4),
+        "roofline": {"kernel": "k_tile (K4 tile raster/ROP, persistent over all frames)", "bound": "hbm",
+                     "achieved": round(achieved, 2) if achieved else None, "peak": peak,
+                     "peak_source": f"{peak_src} (HBM copy)", "unit": "GB/s",
+                     "frac": round(achieved / peak, 5) if achieved else None,
+                     "algorithmic_bytes_per_launch": int(k4_bytes), "traffic": ncu_traffic(spec["name"])},
+        "e2e": {"value": round(e2e_s and e_steps * BATCH_FRAMES / e2e_s, 2), "unit": "frames/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(npix * 4)},
+        "gpu_launches": int(bst["kernel_launches"]),
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_batch_baseline(args.cpu_seconds)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def cpu_batch_frames(lib, scenes, threads):
+    """Render each scene once on the oracle, one context per thread; returns wall seconds."""
+    def one(sc):
+        c = lib.context(sc.width, sc.height)
+        sc.play(c)
+        c.destroy()
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, scenes))
+    return time.perf_counter() - t0
+
+
+def cpu_batch_sample(seconds):
+    """Frames of the uneven batch whose oracle time fits the budget: every k-th frame."""
+    scenes = W.uneven_batch(BATCH_FRAMES, use_vbo=False)
+    tris = [W.scene_triangles(sc) for sc in scenes]
+    per_tri = 2.5e-6  # conservative CPU seconds per input triangle per thread
+    threads = os.cpu_count() or 1
+    k = 1
+    while k < BATCH_FRAMES and sum(tris[::k]) * per_tri / threads > seconds:
+        k *= 2
+    return scenes[::k], k, threads
+
+
+def cpu_batch_baseline(seconds):
+    lib = _oracle_lib()
+    sample, k, threads = cpu_batch_sample(seconds)
+    wall = cpu_batch_frames(lib, sample, threads)
+    return {"value": round(len(sample) / wall, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": (f"every {k}th frame of the 256-frame batch ({len(sample)} frames, whole frames), "
+                       f"one oracle context per frame on {threads} threads"), "wall_s": round(wall, 2)}
+
+
 def _oracle_lib():
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True, capture_output=True)
     return G.load(os.path.join(REPO, "oracle", "_build", "libmtgl_oracle.so"))
@@ -385,6 +614,24 @@ def run_reference(args, spec):
     if rank != 0:
         return None
     lib = _oracle_lib()
+    if spec is WORKLOADS["batch"]:
+        sample, k, threads = cpu_batch_sample(120.0 / max(1, args.steps + args.warmup))
+        for _ in range(args.warmup):
+            cpu_batch_frames(lib, sample, threads)
+        walls = [cpu_batch_frames(lib, sample, threads) for _ in range(args.steps)]
+        fps = len(sample) / statistics.median(walls)
+        desc = (f"every {k}th frame of the 256-frame batch ({len(sample)} whole frames) per step, one oracle "
+                f"context per frame on {threads} threads")
+        return {"impl": "reference", "metric": "frames/s", "value": round(fps, 5), "unit": "frames/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(statistics.median(walls) * 1e3, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded; mytinygl_gb300/workloads.py uneven_batch)",
+                "config": {"workload": spec["name"], "description": spec["desc"]},
+                "cpu_baseline": {"value": round(fps, 5), "unit": "frames/s", "cores": threads, "kind": "port",
+                                 "sample": desc},
+                "e2e": {"value": round(fps, 5), "unit": "frames/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
     threads = os.cpu_count() or 1
     full = spec["full_tris"]
     sample = min(full, 500)
@@ -426,7 +673,12 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
     spec = WORKLOADS[args.workload]
-    out = run_reference(args, spec) if args.impl == "reference" else run_ours(args, spec)
+    if args.impl == "reference":
+        out = run_reference(args, spec)
+    elif args.workload == "batch":
+        out = run_batch(args, spec)
+    else:
+        out = run_ours(args, spec)
     if out is not None:
         print(json.dumps(out), flush=True)
 

@@ -201,6 +201,57 @@ void *mtgl_dev_stream(mtgl_dev *d);
 #define MTGL_OPT_DEPTH_REJECTION 1
 int mtgl_dev_set_option(mtgl_dev *d, int option, int value);
 
+/* ---- batches: many contexts' pending passes in one pipeline run ----
+ *
+ * No counterpart in MyTinyGL, which renders one context at a time inside glEnd. A batch
+ * takes the pending pass (clears, then draws) of each of n contexts of one device, each
+ * with its own framebuffer size and GL state, and renders them all with one run of the
+ * pipeline: one vertex launch, one setup launch, one binning pass over the tiles of all
+ * frames, and one persistent tile launch whose CTAs take (frame, tile) work items from a
+ * device queue, costliest first. The run enqueues without host waits and is captured in a
+ * CUDA graph, replayed while the batch keeps its shape. Every framebuffer ends up exactly
+ * as rendering each context alone would leave it.
+ *
+ * Record and tile-pair buffers have fixed capacities (set from the config, then from the
+ * largest totals seen). A run that exceeds one leaves every framebuffer untouched;
+ * mtgl_dev_batch_wait sees it, grows the capacities and renders the batch again. */
+typedef struct mtgl_batch mtgl_batch;
+
+typedef struct {
+    int32_t tile_size;       /* 8, 16 or 32 pixels; 0: the tuned default                    */
+    int32_t ctas_per_sm;     /* persistent tile CTAs per SM; 0: the tuned default           */
+    float record_factor;     /* initial record capacity per input triangle; 0: default      */
+    float pair_factor;       /* initial tile-pair capacity per record; 0: default           */
+    int32_t use_graph;       /* 1: capture the run in a CUDA graph and replay it; 0: launch */
+    int32_t order_by_cost;   /* 1: hand out the costliest tiles first; 0: in frame order    */
+} mtgl_batch_config;
+
+typedef struct {
+    uint64_t batches, frames, input_triangles, setup_triangles, bin_entries, fragments;
+    uint64_t graph_captures, graph_replays, overflow_reruns, kernel_launches;
+    uint32_t record_capacity, pair_capacity;
+    int32_t tile_size, ctas;
+} mtgl_batch_stats;
+
+/* The defaults mtgl_dev_batch_create uses for zero fields. */
+void mtgl_dev_batch_defaults(mtgl_batch_config *cfg);
+int mtgl_dev_batch_create(const mtgl_batch_config *cfg, mtgl_batch **out);
+int mtgl_dev_batch_destroy(mtgl_batch *b);
+/* Renders the pending pass of each of devs[0..n) (each context at most once) as one
+ * batch and returns without waiting; a previous submission of b is waited for first.
+ * Afterwards each context reads, flushes or changes resources only after the batch. */
+int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n);
+/* Waits for the last submission and checks its capacities (see above). */
+int mtgl_dev_batch_wait(mtgl_batch *b);
+int mtgl_dev_batch_stats(mtgl_batch *b, mtgl_batch_stats *out);
+int mtgl_dev_batch_reset_stats(mtgl_batch *b);
+/* The cudaStream_t the batch runs on. */
+void *mtgl_dev_batch_stream(mtgl_batch *b);
+/* Per-phase device timing of the batch's runs, as mtgl_dev_profile / mtgl_dev_timings.
+ * Runs replayed from a CUDA graph carry no phase events: profile with use_graph = 0. */
+int mtgl_dev_batch_profile(mtgl_batch *b, int enable);
+int mtgl_dev_batch_timings(mtgl_batch *b, mtgl_timings *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,26 @@ int mtgl_set_option(GLState *ctx, int option, int value);
  * the array's address; make it before any stream capture. */
 int mtgl_flush_noalloc(GLState *ctx);
 
+/* Render the pending frame (clears, then draws) of each of ctxs[0..n) in one batch; see
+ * mtgl_dev_batch_submit in mtgl_dev.h. No counterpart in the reference, which renders
+ * each context synchronously. Frames may differ in size and state; every framebuffer ends
+ * up exactly as mtgl_finish on each context alone would leave it. Returns without
+ * waiting; reading a context (glReadPixels, glFinish, mtgl_color_buffer) waits for it. */
+int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n);
+
+/* Replay a GL command stream onto ctx (made current). No counterpart in the reference.
+ * The stream is a sequence of records: u32 function id (the entry point's index among the
+ * gl* functions of GL/gl.h in sorted name order), u32 argument count, then one 8-byte slot
+ * per argument: int64 for integers, enums and pointers, IEEE double for GLfloat and
+ * GLdouble. Each record calls the public entry point, exactly as the application would;
+ * pointers must stay valid for as long as GL may read them. Returns MTGL_ERR_INVALID at
+ * the first malformed record (the calls before it have run). */
+int mtgl_play(GLState *ctx, const void *stream, size_t bytes);
+/* mtgl_play for each (ctxs[i], streams[i]) in order; the current context is restored. */
+int mtgl_play_many(GLState *const *ctxs, const void *const *streams, const size_t *bytes, int32_t n);
+/* number of entry points a stream can call (the function-id range) */
+int mtgl_play_function_count(void);
+
 #ifdef __cplusplus
 }
 #endif

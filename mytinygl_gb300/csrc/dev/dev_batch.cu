@@ -1,0 +1,400 @@
+// dev_batch.cu — batches: the pending passes of many contexts rendered by one pipeline run.
+//
+// No counterpart in the reference (one context renders at a time, inside glEnd). A batch
+// turns n contexts' pending passes into one frame table (dev_pipeline.cu: every frame has
+// its own framebuffer, size, tile range and clears; every draw keeps its own state
+// blocks) and runs the pipeline once: K1 over all vertices, K2 over all triangles, K3 over
+// the tiles of all frames, and a persistent K4 whose CTAs drain a device queue of
+// (frame, tile) items ordered costliest first. The run has no host waits (record and pair
+// buffers have fixed capacities, checked on the device), so it is captured once as a CUDA
+// graph and replayed for as long as the batch's shape (tables, capacities, buffers) stays
+// the same; only the staged bytes change between replays.
+#include <algorithm>
+#include <new>
+
+#include "dev_internal.h"
+#include "tuned.h"
+
+using namespace mtgl;
+
+namespace {
+
+// launch shape the graph was captured with: a replay is valid while every field matches
+struct Signature {
+    const void *dstage, *hstage;
+    size_t staged;
+    Tables t;
+    uint32_t rec_cap, pair_cap;
+    int32_t ctas;
+    int32_t order;
+    void *scratch[kScratchSlots];
+};
+
+bool same(const Signature &a, const Signature &b) { return memcmp(&a, &b, sizeof(a)) == 0; }
+
+// capacities are rounded up to 1/8 of their power-of-two size (at least 256 entries), so
+// small changes between submissions keep the same capacity and the same graph
+uint32_t round_capacity(uint64_t v)
+{
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    const uint64_t q = std::max<uint64_t>(256, p / 8);
+    const uint64_t r = (v + q - 1) / q * q;
+    return (uint32_t)std::min<uint64_t>(r, 0xFFFFFF00ull);
+}
+
+}  // namespace
+
+struct mtgl_batch {
+    Exec x;
+    HostStage stage;
+    mtgl_batch_config cfg{};
+    int tile_shift = 4;
+    uint32_t rec_cap = 0, pair_cap = 0;  // capacities learned from the totals seen so far
+    cudaEvent_t done = nullptr;
+    // the submission in flight
+    bool pending = false;
+    std::vector<mtgl_dev *> devs;
+    std::vector<Pass> passes;
+    std::vector<FrameSrc> frames;
+    Tables t;
+    PipeConfig run{};
+    // graph of the last capacity-mode run
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    Signature sig{};
+    bool have_sig = false;
+    int graph_launches_ = 0;  // kernels one replay launches
+    mtgl_batch_stats stats{};
+};
+
+namespace {
+
+int record_after(mtgl_batch *b)
+{
+    for (mtgl_dev *d : b->devs) {
+        CK(cudaEventRecord(d->after_batch, b->x.stream));
+        d->wait_batch = true;
+    }
+    CK(cudaEventRecord(b->done, b->x.stream));
+    return MTGL_OK;
+}
+
+int persistent_ctas(mtgl_batch *b, const Tables &t)
+{
+    TileArgs probe;
+    memset(&probe, 0, sizeof(probe));
+    probe.tile_shift = t.tile_shift;
+    probe.any_texture = t.any_texture ? 1 : 0;
+    probe.eye_records = t.eye ? reinterpret_cast<const float *>(1) : nullptr;
+    const int occ = tile_occupancy(probe);
+    const int per_sm = b->cfg.ctas_per_sm > 0 ? std::min(b->cfg.ctas_per_sm, occ) : occ;
+    return std::max(1, per_sm) * b->x.sms;
+}
+
+int launch_run(mtgl_batch *b)
+{
+    const bool was_profiling = b->x.profile;
+    if (b->cfg.use_graph) b->x.profile = false;  // phase events would be baked into the graph
+    int st = run_pipeline(b->x, b->x.pool, b->stage, b->t, b->run, nullptr, true);  // scratch first
+    if (st) return st;
+    Signature s;
+    memset(&s, 0, sizeof(s));
+    s.dstage = b->x.dstage;
+    s.hstage = b->stage.p;
+    s.staged = b->stage.used;
+    s.t = b->t;
+    s.rec_cap = b->run.rec_cap;
+    s.pair_cap = b->run.pair_cap;
+    s.ctas = b->run.ctas;
+    s.order = b->run.order ? 1 : 0;
+    for (int i = 0; i < kScratchSlots; i++) s.scratch[i] = b->x.pool.p[i];
+    if (!b->cfg.use_graph) {
+        PipeOut o;
+        st = run_pipeline(b->x, b->x.pool, b->stage, b->t, b->run, &o);
+        b->stats.kernel_launches += (uint64_t)o.launches;
+        b->x.profile = was_profiling;
+        return st;
+    }
+    if (!(b->exec && b->have_sig && same(s, b->sig))) {
+        CK(cudaStreamBeginCapture(b->x.stream, cudaStreamCaptureModeThreadLocal));
+        PipeOut o;
+        st = run_pipeline(b->x, b->x.pool, b->stage, b->t, b->run, &o);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->x.stream, &g);
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return fail_cuda("cudaStreamEndCapture", e);
+        bool updated = false;
+        if (b->exec) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(b->exec, g, &info) == cudaSuccess;
+            if (!updated) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(b->exec);
+                b->exec = nullptr;
+            }
+        }
+        if (!updated) CK(cudaGraphInstantiate(&b->exec, g, 0));
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->graph = g;
+        b->sig = s;
+        b->have_sig = true;
+        b->stats.graph_captures++;
+        b->stats.kernel_launches += (uint64_t)o.launches;
+        b->graph_launches_ = o.launches;
+    } else {
+        b->stats.graph_replays++;
+        b->stats.kernel_launches += (uint64_t)b->graph_launches_;
+    }
+    CK(cudaGraphLaunch(b->exec, b->x.stream));
+    b->x.profile = was_profiling;
+    return MTGL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mtgl_dev_batch_defaults(mtgl_batch_config *cfg)
+{
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->tile_size = MTGL_TUNED_TILE_SIZE;
+    cfg->ctas_per_sm = MTGL_TUNED_CTAS_PER_SM;
+    cfg->record_factor = MTGL_TUNED_RECORD_FACTOR;
+    cfg->pair_factor = MTGL_TUNED_PAIR_FACTOR;
+    cfg->use_graph = 1;
+    cfg->order_by_cost = 1;
+}
+
+int mtgl_dev_batch_create(const mtgl_batch_config *cfg, mtgl_batch **out)
+{
+    if (!out) return MTGL_ERR_INVALID;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        snprintf(g_err, sizeof(g_err), "no CUDA device (%s)", e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+        return MTGL_ERR_NO_DEVICE;
+    }
+    mtgl_batch_config c;
+    mtgl_dev_batch_defaults(&c);
+    if (cfg) {
+        if (cfg->tile_size) c.tile_size = cfg->tile_size;
+        if (cfg->ctas_per_sm) c.ctas_per_sm = cfg->ctas_per_sm;
+        if (cfg->record_factor > 0) c.record_factor = cfg->record_factor;
+        if (cfg->pair_factor > 0) c.pair_factor = cfg->pair_factor;
+        c.use_graph = cfg->use_graph;
+        c.order_by_cost = cfg->order_by_cost;
+    }
+    int shift = 0;
+    while (shift <= kTileShiftMax && (1 << shift) != c.tile_size) shift++;
+    if (shift < kTileShiftMin || shift > kTileShiftMax || c.ctas_per_sm < 0) return MTGL_ERR_INVALID;
+    mtgl_batch *b = new (std::nothrow) mtgl_batch();
+    if (!b) return MTGL_ERR_OOM;
+    b->cfg = c;
+    b->tile_shift = shift;
+    int st = b->x.init(nullptr);
+    if (st) {
+        delete b;
+        return st;
+    }
+    CK(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    b->stats.tile_size = c.tile_size;
+    *out = b;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_destroy(mtgl_batch *b)
+{
+    if (!b) return MTGL_OK;
+    cudaSetDevice(b->x.device);
+    mtgl_dev_batch_wait(b);
+    cudaStreamSynchronize(b->x.stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->stage.release();
+    b->x.destroy();
+    cudaEventDestroy(b->done);
+    delete b;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
+{
+    if (!b || n < 0 || (n > 0 && !devs)) return MTGL_ERR_INVALID;
+    CK(cudaSetDevice(b->x.device));
+    int st = mtgl_dev_batch_wait(b);
+    if (st) return st;
+    for (int32_t i = 0; i < n; i++) {
+        mtgl_dev *d = devs[i];
+        if (!d || d->device != b->x.device) return MTGL_ERR_INVALID;
+        for (int32_t j = 0; j < i; j++)
+            if (devs[j] == d) return MTGL_ERR_INVALID;  // a context renders one pass per batch
+        if (d->batch && (st = mtgl_dev_batch_wait(d->batch))) return st;
+    }
+    if ((st = b->stage.wait())) return st;
+    b->stage.used = 0;
+    b->devs.clear();
+    b->passes.clear();
+    b->frames.clear();
+    b->passes.reserve((size_t)n);
+    uint64_t tris = 0;
+    for (int32_t i = 0; i < n; i++) {
+        mtgl_dev *d = devs[i];
+        if (d->pass.empty()) continue;
+        // order the batch after work already queued on the context's stream, and after a
+        // batch of another executor the context's stream has not waited for yet
+        if (d->dirty) {
+            CK(cudaEventRecord(d->tail, d->x.stream));
+            CK(cudaStreamWaitEvent(b->x.stream, d->tail, 0));
+            d->dirty = false;
+        }
+        if (d->wait_batch) CK(cudaStreamWaitEvent(b->x.stream, d->after_batch, 0));
+        int64_t off = 0;
+        if ((st = b->stage.reserve(d->stage.used, &off))) return st;
+        if (d->stage.used) memcpy(b->stage.p + off, d->stage.p, d->stage.used);
+        b->passes.push_back(std::move(d->pass));
+        d->pass.reset();
+        d->stage.used = 0;
+        b->devs.push_back(d);
+        b->frames.push_back(FrameSrc{d, nullptr, off});
+        tris += b->passes.back().tris;
+        d->stats.passes++;
+        d->stats.input_triangles += b->passes.back().tris;
+    }
+    if (b->devs.empty()) return MTGL_OK;
+    for (size_t i = 0; i < b->frames.size(); i++) b->frames[i].pass = &b->passes[i];
+    if ((st = build_tables(b->x, b->stage, b->frames.data(), (uint32_t)b->frames.size(), b->tile_shift, true, b->t)))
+        return st;
+
+    // capacities: the larger of the learned totals and the configured factors
+    const uint64_t rec_want = std::max<uint64_t>((uint64_t)b->rec_cap, (uint64_t)(tris * b->cfg.record_factor) + 1);
+    const uint32_t rec_cap = tris ? round_capacity(rec_want) : 0;
+    const uint64_t pair_want = std::max<uint64_t>((uint64_t)b->pair_cap, (uint64_t)(rec_cap * b->cfg.pair_factor) + 1);
+    const uint32_t pair_cap = tris ? round_capacity(pair_want) : 0;
+    b->run = PipeConfig();
+    b->run.exact = false;
+    b->run.rec_cap = rec_cap;
+    b->run.pair_cap = pair_cap;
+    b->run.ctas = persistent_ctas(b, b->t);
+    b->run.order = b->cfg.order_by_cost != 0;
+    if ((st = launch_run(b))) return st;
+    if ((st = b->stage.mark_uploaded(b->x.stream))) return st;
+    if ((st = record_after(b))) return st;
+    for (mtgl_dev *d : b->devs) d->batch = b;
+    b->pending = true;
+    b->stats.batches++;
+    b->stats.frames += b->devs.size();
+    b->stats.input_triangles += tris;
+    b->stats.ctas = b->run.ctas;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_wait(mtgl_batch *b)
+{
+    if (!b) return MTGL_ERR_INVALID;
+    if (!b->pending) return MTGL_OK;
+    CK(cudaSetDevice(b->x.device));
+    b->pending = false;  // a failure below leaves nothing to retry
+    for (mtgl_dev *d : b->devs) d->batch = nullptr;
+    CK(cudaEventSynchronize(b->done));
+    uint32_t nrec = b->x.h_totals[0], npairs = b->x.h_totals[1];
+    if (nrec > b->run.rec_cap || npairs > b->run.pair_cap) {
+        // The tile launch left every framebuffer untouched: render again with exact sizing
+        // from the same staged tables, and remember the totals for the next submission.
+        PipeConfig c = b->run;
+        c.exact = true;
+        PipeOut o;
+        int st = run_pipeline(b->x, b->x.pool, b->stage, b->t, c, &o);
+        if (st) return st;
+        if ((st = b->stage.mark_uploaded(b->x.stream))) return st;
+        if ((st = record_after(b))) return st;
+        CK(cudaEventSynchronize(b->done));
+        nrec = o.nrec;
+        npairs = o.npairs;
+        b->stats.overflow_reruns++;
+        b->stats.kernel_launches += (uint64_t)o.launches;
+    }
+    b->rec_cap = std::max(b->rec_cap, nrec);
+    b->pair_cap = std::max(b->pair_cap, npairs);
+    b->stats.setup_triangles += nrec;
+    b->stats.bin_entries += npairs;
+    b->stats.record_capacity = b->run.rec_cap;
+    b->stats.pair_capacity = b->run.pair_cap;
+    b->devs.clear();
+    b->passes.clear();
+    b->frames.clear();
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_stats(mtgl_batch *b, mtgl_batch_stats *out)
+{
+    if (!b || !out) return MTGL_ERR_INVALID;
+    int st = mtgl_dev_batch_wait(b);
+    if (st) return st;
+    unsigned long long f = 0;
+    CK(cudaMemcpyAsync(&f, b->x.d_frags, sizeof(f), cudaMemcpyDeviceToHost, b->x.stream));
+    CK(cudaStreamSynchronize(b->x.stream));
+    *out = b->stats;
+    out->fragments = f;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_reset_stats(mtgl_batch *b)
+{
+    if (!b) return MTGL_ERR_INVALID;
+    int st = mtgl_dev_batch_wait(b);
+    if (st) return st;
+    const int32_t ts = b->stats.tile_size, ctas = b->stats.ctas;
+    memset(&b->stats, 0, sizeof(b->stats));
+    b->stats.tile_size = ts;
+    b->stats.ctas = ctas;
+    CK(cudaMemsetAsync(b->x.d_frags, 0, sizeof(unsigned long long), b->x.stream));
+    CK(cudaStreamSynchronize(b->x.stream));
+    return MTGL_OK;
+}
+
+void *mtgl_dev_batch_stream(mtgl_batch *b) { return b ? (void *)b->x.stream : nullptr; }
+
+int mtgl_dev_batch_profile(mtgl_batch *b, int enable)
+{
+    if (!b) return MTGL_ERR_INVALID;
+    int st = mtgl_dev_batch_wait(b);
+    if (st) return st;
+    CK(cudaStreamSynchronize(b->x.stream));
+    if ((st = b->x.prof_collect())) return st;
+    b->x.profile = enable != 0;
+    memset(&b->x.timings, 0, sizeof(b->x.timings));
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_timings(mtgl_batch *b, mtgl_timings *out)
+{
+    if (!b || !out) return MTGL_ERR_INVALID;
+    int st = mtgl_dev_batch_wait(b);
+    if (st) return st;
+    CK(cudaStreamSynchronize(b->x.stream));
+    if ((st = b->x.prof_collect())) return st;
+    *out = b->x.timings;
+    return MTGL_OK;
+}
+
+}  // extern "C"
+
+// ---- GL-level entry: the contexts' pending frames as one batch
+
+extern "C" mtgl_dev *fe_context_device(GLState *ctx);
+
+extern "C" int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n)
+{
+    if (!b || n < 0 || (n > 0 && !ctxs)) return MTGL_ERR_INVALID;
+    std::vector<mtgl_dev *> devs((size_t)n);
+    for (int32_t i = 0; i < n; i++) {
+        devs[i] = ctxs[i] ? fe_context_device(ctxs[i]) : nullptr;
+        if (!devs[i]) return MTGL_ERR_INVALID;
+    }
+    return mtgl_dev_batch_submit(b, devs.data(), n);
+}

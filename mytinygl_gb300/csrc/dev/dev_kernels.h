@@ -19,7 +19,8 @@ struct GeomArgs {
     PostEye *eyes;                    // null when no draw of the pass lights per fragment
     uint32_t total_slots;
     uint32_t total_tris;
-    FrameDims dims;
+    const DevFrame *frames;           // the raster state's `frame` indexes this table
+    uint32_t nframes;
     uint32_t *tri_counts;             // count pass output
     const uint32_t *tri_offsets;      // emit pass input (exclusive scan of tri_counts)
     float *records;                   // emit pass output, kRecWords per record
@@ -41,10 +42,17 @@ int launch_setup_emit(const GeomArgs &a, cudaStream_t s);
 size_t scan_temp_words(uint32_t n);
 int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, uint32_t *total_dev, cudaStream_t s);
 
+// Element counts of the binning stage live on the device (written by the scans), so the
+// stage runs without the host knowing them. `nrec` / `npairs` on the host are capacities:
+// they size grids and buffers, and kernels read the real counts through nrec_dev / total_dev.
 struct BinArgs {
     const float *records;
-    uint32_t nrec;
-    FrameDims dims;
+    uint32_t nrec;              // record capacity
+    const uint32_t *nrec_dev;   // records written (may exceed nrec: the excess was dropped)
+    const DevFrame *frames;
+    uint32_t nframes;
+    int32_t tile_shift;         // tile edge = 1 << tile_shift
+    uint32_t ntiles;            // tiles of all frames
     uint32_t *rec_tiles;        // per record tile count, then its exclusive scan (in place)
     uint32_t *keys, *vals;      // pair buffers (capacity >= pairs)
     uint32_t *keys_alt, *vals_alt;
@@ -52,17 +60,25 @@ struct BinArgs {
     uint32_t *tile_start;       // exclusive scan of tile_count
     uint32_t *radix_hist;       // radix histograms
     uint32_t *scan_temp;
-    uint32_t *total_dev;
-    uint32_t npairs;            // set by the host after the count scan
-    uint32_t pairs_cap;         // pair capacity of keys/vals (writes beyond are dropped)
+    uint32_t *total_dev;        // where the pair scan writes its total: the pairs generated
+    uint32_t *sort_total_dev;   // a word the sort's histogram scans may overwrite
+    uint32_t npairs;            // pair capacity of keys/vals (writes beyond are dropped)
+    int32_t sms;                // SMs of the device (grid sizes)
 };
 
 int launch_bin_count(const BinArgs &a, cudaStream_t s);
 int launch_bin_expand(const BinArgs &a, cudaStream_t s);
-// Stable sort of (tile, record) pairs by tile; result in keys/vals. Returns nothing; uses
-// keys_alt/vals_alt as ping-pong storage.
+// Stable sort of (tile, record) pairs by tile; result in keys/vals. Uses keys_alt/vals_alt
+// as ping-pong storage.
 int launch_bin_sort(BinArgs &a, cudaStream_t s);
 size_t radix_hist_words(uint32_t npairs);
+
+// Work order of a persistent tile launch: tile ids by descending record count (coarse
+// log buckets), so the longest tiles start first. order holds ntiles words, hist
+// kOrderHistWords.
+int launch_tile_order(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist, uint32_t *order, int sms,
+                      cudaStream_t s);
+constexpr size_t kOrderHistWords = 512;
 
 struct TileArgs {
     const float *records;
@@ -72,19 +88,27 @@ struct TileArgs {
     const uint32_t *tile_count;
     const DevRaster *rasters;
     uint32_t nrasters;
-    const ClearOp *clears;
-    int32_t nclears;
+    const ClearOp *clears;       // all frames' clears; a frame holds its range
+    const DevFrame *frames;
+    uint32_t nframes;
+    uint32_t ntiles;             // work items: global tile ids
+    const uint32_t *order;       // item -> tile (null: item i is tile i)
+    uint32_t *queue;             // work-queue head, zero at launch
+    int32_t ctas;                // persistent CTAs (0: one per tile)
+    int32_t tile_shift;
     int32_t any_texture;         // some raster state of the pass samples a texture
-    FrameDims dims;
-    uint32_t *color;
-    float *depth;
-    uint8_t *stencil;
+    // capacity check: when guard[0] > records_cap or guard[1] > pairs_cap the binning
+    // dropped entries, and the launch leaves every framebuffer untouched
+    const uint32_t *guard;
+    uint32_t records_cap, pairs_cap;
     unsigned long long *fragments;
 };
 
-// K4: one CTA per 16x16 tile: clears, then every triangle of the tile in order through the
-// full fragment pipeline (raster.c:532-724), then one write-back.
+// K4: CTAs take tiles from the work queue; for each: clears, then every triangle of the
+// tile in order through the full fragment pipeline (raster.c:532-724), then one write-back.
 int launch_tile(const TileArgs &a, cudaStream_t s);
+// resident CTAs per SM of the K4 variant a launch with these arguments uses
+int tile_occupancy(const TileArgs &a);
 
 // glClear without draws (gl_api.c:409-457)
 void launch_clear(const ClearOp *ops_host, int nops, FrameDims dims, uint32_t *color, float *depth, uint8_t *stencil,

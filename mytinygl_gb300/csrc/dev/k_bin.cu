@@ -1,11 +1,13 @@
 // k_bin.cu — K3 binning: triangle records -> per-tile lists in submission order.
 //
 // No counterpart in the reference, which scans every triangle's bounding box on one thread
-// (raster.c:532-724). Here each record is expanded into one (tile, record) pair per 16x16
-// tile its clamped bounding box touches; pairs are generated in submission order and a
+// (raster.c:532-724). Here each record is expanded into one (tile, record) pair per tile
+// (8, 16 or 32 pixels square) its clamped bounding box touches; pairs are generated in submission order and a
 // stable LSD radix sort on the tile id (warp match-any ranking plus prefix sums) groups
 // them by tile while keeping that order inside every tile. The tile kernel then walks each
 // list front to back, so blending and stencil updates happen in GL order.
+#include <algorithm>
+
 #include "dev_kernels.h"
 
 namespace mtgl {
@@ -111,62 +113,146 @@ int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, u
 
 // ------------------------------------------------------------------ record -> tiles
 
-// The setup kernel clamps every bbox to the framebuffer; the clamps here only keep tile
-// indices inside the tile grid whatever a record holds.
-__device__ __forceinline__ void rec_tile_box(const float *rec, const FrameDims &dims, int &tx0, int &ty0, int &tx1,
-                                             int &ty1)
+// The setup kernel clamps every bbox to its framebuffer; the clamps here only keep tile
+// indices inside the frame's tile grid whatever a record holds. Returns the frame.
+__device__ __forceinline__ const DevFrame &rec_tile_box(const float *rec, const BinArgs &A, int &tx0, int &ty0,
+                                                        int &tx1, int &ty1)
 {
     const float4 b1 = __ldg(reinterpret_cast<const float4 *>(rec) + 1);
     const float4 b2 = __ldg(reinterpret_cast<const float4 *>(rec) + 2);
-    tx0 = min(max(__float_as_int(b1.z), 0), dims.width - 1) / kTile;
-    ty0 = min(max(__float_as_int(b1.w), 0), dims.height - 1) / kTile;
-    tx1 = max(min(__float_as_int(b2.x), dims.width - 1) / kTile, tx0);
-    ty1 = max(min(__float_as_int(b2.y), dims.height - 1) / kTile, ty0);
+    const uint32_t f = min(__float_as_uint(__ldg(rec + R_FRAME)), A.nframes - 1);
+    const DevFrame &F = A.frames[f];
+    const int sh = A.tile_shift;
+    tx0 = min(max(__float_as_int(b1.z), 0), F.dims.width - 1) >> sh;
+    ty0 = min(max(__float_as_int(b1.w), 0), F.dims.height - 1) >> sh;
+    tx1 = max(min(__float_as_int(b2.x), F.dims.width - 1) >> sh, tx0);
+    ty1 = max(min(__float_as_int(b2.y), F.dims.height - 1) >> sh, ty0);
+    return F;
 }
 
+__device__ __forceinline__ uint32_t records_in(const BinArgs &A) { return min(*A.nrec_dev, A.nrec); }
+
+// tiles per record; records past the real count get 0 so the scan over the capacity is exact
 __global__ void __launch_bounds__(256) k_bin_count(BinArgs A)
 {
-    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= A.nrec) return;
-    int tx0, ty0, tx1, ty1;
-    rec_tile_box(A.records + (size_t)r * kRecWords, A.dims, tx0, ty0, tx1, ty1);
-    A.rec_tiles[r] = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+    const uint32_t n = records_in(A);
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < A.nrec; r += gridDim.x * blockDim.x) {
+        uint32_t c = 0;
+        if (r < n) {
+            int tx0, ty0, tx1, ty1;
+            rec_tile_box(A.records + (size_t)r * kRecWords, A, tx0, ty0, tx1, ty1);
+            c = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+        }
+        A.rec_tiles[r] = c;
+    }
 }
 
 // one warp per record: lanes write the record's tiles row-major (pairs stay in submission order)
 __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
 {
-    const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t n = records_in(A);
     const int lane = threadIdx.x & 31;
-    if (r >= A.nrec) return;
-    int tx0, ty0, tx1, ty1;
-    rec_tile_box(A.records + (size_t)r * kRecWords, A.dims, tx0, ty0, tx1, ty1);
-    const int w = tx1 - tx0 + 1;
-    const int cnt = w * (ty1 - ty0 + 1);
-    const uint32_t base = A.rec_tiles[r];
-    for (int i = lane; i < cnt; i += 32) {
-        if (base + (uint32_t)i >= A.pairs_cap) break;
-        const int tx = tx0 + i % w, ty = ty0 + i / w;
-        const uint32_t tile = (uint32_t)(ty * A.dims.tiles_x + tx);
-        A.keys[base + i] = tile;
-        A.vals[base + i] = r;
-        atomicAdd(A.tile_count + tile, 1u);
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        int tx0, ty0, tx1, ty1;
+        const DevFrame &F = rec_tile_box(A.records + (size_t)r * kRecWords, A, tx0, ty0, tx1, ty1);
+        const int w = tx1 - tx0 + 1;
+        const int cnt = w * (ty1 - ty0 + 1);
+        const uint32_t base = A.rec_tiles[r];
+        for (int i = lane; i < cnt; i += 32) {
+            if (base + (uint32_t)i >= A.npairs) break;
+            const int tx = tx0 + i % w, ty = ty0 + i / w;
+            const uint32_t tile = F.tile_base + (uint32_t)(ty * F.dims.tiles_x + tx);
+            A.keys[base + i] = tile;
+            A.vals[base + i] = r;
+            atomicAdd(A.tile_count + tile, 1u);
+        }
     }
+}
+
+// grids cover the work or the GPU (16 CTAs per SM), whichever is smaller; kernels loop over the rest
+unsigned stride_grid(uint64_t threads, unsigned block, int sms)
+{
+    const uint64_t want = (threads + block - 1) / block;
+    const uint64_t cap = (uint64_t)(sms > 0 ? sms : 1) * 16;
+    return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
 }
 
 int launch_bin_count(const BinArgs &a, cudaStream_t s)
 {
     if (!a.nrec) return 0;
-    k_bin_count<<<(a.nrec + 255) / 256, 256, 0, s>>>(a);
+    k_bin_count<<<stride_grid(a.nrec, 256, a.sms), 256, 0, s>>>(a);
     return 1;
 }
 
 int launch_bin_expand(const BinArgs &a, cudaStream_t s)
 {
     if (!a.nrec) return 0;
-    const uint64_t threads = (uint64_t)a.nrec * 32;
-    k_bin_expand<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a);
+    k_bin_expand<<<stride_grid((uint64_t)a.nrec * 32, 256, a.sms), 256, 0, s>>>(a);
     return 1;
+}
+
+// ------------------------------------------------------------------ persistent work order
+
+// coarse log2 bucket of a tile's record count: 8 steps per octave, 0 for an empty tile
+__device__ __forceinline__ uint32_t cost_bucket(uint32_t c)
+{
+    if (c == 0) return 0;
+    const int lg = 31 - __clz(c);
+    const uint32_t frac = lg >= 3 ? (c >> (lg - 3)) & 7u : (c << (3 - lg)) & 7u;
+    return min(1u + (uint32_t)lg * 8u + frac, 255u);
+}
+
+// hist[0..255]: tiles per bucket; hist[256..511]: placement cursors (both zero at launch)
+__global__ void __launch_bounds__(256) k_order_hist(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist)
+{
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+        atomicAdd(&h[cost_bucket(tile_count[t])], 1u);
+    __syncthreads();
+    if (h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+// Places every tile after all tiles of costlier buckets. The order inside a bucket is
+// whatever the atomics give: tiles are independent, so the order changes timing only.
+__global__ void __launch_bounds__(256) k_order_scatter(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist,
+                                                       uint32_t *order)
+{
+    __shared__ uint32_t start[256];
+    __shared__ uint32_t warp_tot[8];
+    // exclusive prefix over buckets in descending order: bucket b starts after buckets > b
+    const int b = 255 - (int)threadIdx.x;
+    const uint32_t v = hist[b];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; w++) before += warp_tot[w];
+    start[b] = before + x - v;
+    __syncthreads();
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+        const uint32_t bk = cost_bucket(tile_count[t]);
+        order[start[bk] + atomicAdd(&hist[256 + bk], 1u)] = t;
+    }
+}
+
+int launch_tile_order(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist, uint32_t *order, int sms,
+                      cudaStream_t s)
+{
+    if (!ntiles) return 0;
+    cudaMemsetAsync(hist, 0, kOrderHistWords * sizeof(uint32_t), s);
+    const unsigned g = stride_grid(ntiles, 256, sms);
+    k_order_hist<<<g, 256, 0, s>>>(tile_count, ntiles, hist);
+    k_order_scatter<<<g, 256, 0, s>>>(tile_count, ntiles, hist, order);
+    return 2;
 }
 
 // ------------------------------------------------------------------ stable radix sort by tile
@@ -183,9 +269,11 @@ size_t radix_hist_words(uint32_t npairs)
     return nb * kRadixDigits + 64;
 }
 
-__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t *keys, uint32_t n, int shift,
-                                                             uint32_t mask, uint32_t *hist, uint32_t nblocks)
+__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t *keys, uint32_t cap,
+                                                             const uint32_t *n_dev, int shift, uint32_t mask,
+                                                             uint32_t *hist, uint32_t nblocks)
 {
+    const uint32_t n = min(*n_dev, cap);
     __shared__ uint32_t h[kRadixDigits];
     for (int i = threadIdx.x; i < kRadixDigits; i += kRadixThreads) h[i] = 0;
     __syncthreads();
@@ -203,11 +291,13 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t *ke
 // order; match-any groups equal digits, the leader advances the warp's digit counter, and
 // per-digit prefix sums over warps and blocks place every item after all earlier ones.
 __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t *keys, const uint32_t *vals,
-                                                                uint32_t n, int shift, uint32_t mask,
+                                                                uint32_t cap, const uint32_t *n_dev, int shift,
+                                                                uint32_t mask,
                                                                 const uint32_t *hist_scan, uint32_t nblocks,
                                                                 uint32_t *keys_out, uint32_t *vals_out)
 {
     __shared__ uint32_t wcount[kRadixWarps][kRadixDigits];
+    const uint32_t n = min(*n_dev, cap);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kRadixWarps * kRadixDigits; i += kRadixThreads) (&wcount[0][0])[i] = 0;
     __syncthreads();
@@ -254,20 +344,19 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t 
 
 int launch_bin_sort(BinArgs &a, cudaStream_t s)
 {
-    const uint32_t n = a.npairs;
-    if (n <= 1) return 0;
+    const uint32_t n = a.npairs;  // capacity; the kernels read the real count from total_dev
+    if (n == 0) return 0;
     int launches = 0;
-    const uint32_t ntiles = (uint32_t)(a.dims.tiles_x * a.dims.tiles_y);
     int bits = 1;
-    while (bits < 32 && (1u << bits) < ntiles) bits++;
+    while (bits < 32 && (1u << bits) < a.ntiles) bits++;
     const uint32_t nb = (n + kRadixTile - 1) / kRadixTile;
     for (int shift = 0; shift < bits; shift += 8) {
         const int nbits = (bits - shift) < 8 ? (bits - shift) : 8;
         const uint32_t mask = (1u << nbits) - 1u;
-        k_radix_hist<<<nb, kRadixThreads, 0, s>>>(a.keys, n, shift, mask, a.radix_hist, nb);
-        launches += 2 + launch_scan(a.radix_hist, a.radix_hist, nb * kRadixDigits, a.scan_temp, a.total_dev, s);
-        k_radix_scatter<<<nb, kRadixThreads, 0, s>>>(a.keys, a.vals, n, shift, mask, a.radix_hist, nb, a.keys_alt,
-                                                     a.vals_alt);
+        k_radix_hist<<<nb, kRadixThreads, 0, s>>>(a.keys, n, a.total_dev, shift, mask, a.radix_hist, nb);
+        launches += 2 + launch_scan(a.radix_hist, a.radix_hist, nb * kRadixDigits, a.scan_temp, a.sort_total_dev, s);
+        k_radix_scatter<<<nb, kRadixThreads, 0, s>>>(a.keys, a.vals, n, a.total_dev, shift, mask, a.radix_hist, nb,
+                                                     a.keys_alt, a.vals_alt);
         uint32_t *tk = a.keys, *tv = a.vals;
         a.keys = a.keys_alt;
         a.vals = a.vals_alt;

@@ -377,8 +377,9 @@ __device__ __forceinline__ float depth_lower_bound(const DevRaster &R, float z0,
 
 // Per fan triangle: the setup half of rasterize_triangle_smooth. Returns true when the
 // triangle produces a record; writes it when `rec` is non-null.
-__device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raster_id, const FrameDims &dims, const CV &a,
-                                              const CV &b, const CV &c, float *rec, float *eyerec)
+__device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raster_id, uint32_t frame,
+                                              const FrameDims &dims, const CV &a, const CV &b, const CV &c, float *rec,
+                                              float *eyerec)
 {
     const mtgl_raster_state &rs = R.rs;
     int32_t x0, y0, x1, y1, x2, y2;
@@ -456,7 +457,7 @@ __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raste
                          ds.depth_func == GL_ALWAYS);
     const uint32_t flags = (back ? 1u : 0u) | (zc << 1) | (raises ? kFlagRaisesDepth : 0u);
     r4[12] = make_float4(__uint_as_float(flags), fy2 - fy1, fx2 - fx1, fy0 - fy2);
-    r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, 0.0f);
+    r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, __uint_as_float(frame));
     if (eyerec) {
         float4 *e4 = reinterpret_cast<float4 *>(eyerec);
         e4[0] = make_float4(a.ep.x, a.ep.y, a.ep.z, a.en.x);
@@ -480,6 +481,8 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
     element_triple(D.mode, k, e0, e1, e2);
     const DevRaster &R = A.rasters[D.raster];
     const bool eye = R.needs_eye && A.eyes;
+    const uint32_t frame = min(R.frame, A.nframes - 1);
+    const FrameDims dims = A.frames[frame].dims;
 
     CV v0, v1, v2;
     load_cv(A, element_slot(D, e0), eye, v0);
@@ -502,7 +505,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
         const bool room = out < A.records_cap;
         float *rec = (EMIT && room) ? A.records + (size_t)out * kRecWords : nullptr;
         float *erec = (write_eye && room) ? A.eye_records + (size_t)out * kEyeWords : nullptr;
-        if ((EMIT && !room) || setup_fan_tri(R, D.raster, A.dims, v0, v1, v2, rec, erec)) produced = 1;
+        if ((EMIT && !room) || setup_fan_tri(R, D.raster, frame, dims, v0, v1, v2, rec, erec)) produced = 1;
     } else {
         CV bufA[kClipMax], bufB[kClipMax];
         bufA[0] = v0;
@@ -516,7 +519,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
                 if (EMIT && !room) break;
                 float *rec = EMIT ? A.records + (size_t)(out + produced) * kRecWords : nullptr;
                 float *erec = write_eye ? A.eye_records + (size_t)(out + produced) * kEyeWords : nullptr;
-                if (setup_fan_tri(R, D.raster, A.dims, bufA[0], bufA[j], bufA[j + 1], rec, erec)) produced++;
+                if (setup_fan_tri(R, D.raster, frame, dims, bufA[0], bufA[j], bufA[j + 1], rec, erec)) produced++;
             }
         }
     }

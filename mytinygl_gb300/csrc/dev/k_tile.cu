@@ -1,16 +1,22 @@
 // k_tile.cu — K4 tile raster/ROP (replaces rasterize_triangle_smooth's pixel loop,
 // raster.c:532-724, and glClear's loops, gl_api.c:409-457).
 //
-// One CTA owns one 16x16 tile; thread t owns one pixel for the whole pass, so the pixel's
-// colour, depth and stencil stay in registers between triangles. Each warp covers an 8x4
-// block of the tile. The CTA walks the tile's record list (submission order, built by the
-// binning pass) in chunks staged through shared memory; every thread runs the reference's
-// fragment pipeline for its own pixel: edge functions at the integer pixel position,
-// barycentrics, stencil test/ops, depth test, colour (flat / smooth / per-fragment
-// lighting), texture with alpha test and texenv, fog, depth write, blend, masked write.
-// Because a pixel is only ever touched by its own thread, in-order blending and stencil
-// updates need no atomics. Clears of the pass are applied first; a clear that covers the
-// whole tile means that buffer is never read from memory.
+// A CTA owns one tile (8, 16 or 32 pixels square) at a time; thread t owns one pixel for
+// the whole pass, so the pixel's colour, depth and stencil stay in registers between
+// triangles. Each warp covers an 8x4 block of the tile. The CTA walks the tile's record
+// list (submission order, built by the binning pass) in chunks staged through shared
+// memory; every thread runs the reference's fragment pipeline for its own pixel: edge
+// functions at the integer pixel position, barycentrics, stencil test/ops, depth test,
+// colour (flat / smooth / per-fragment lighting), texture with alpha test and texenv, fog,
+// depth write, blend, masked write. Because a pixel is only ever touched by its own thread,
+// in-order blending and stencil updates need no atomics. Clears of the pass are applied
+// first; a clear that covers the whole tile means that buffer is never read from memory.
+//
+// The launch is persistent: CTAs take tiles from a work queue (an atomic head over a list
+// of global tile ids, costliest first in batches) until it is empty, so frames of very
+// different sizes share one launch without idle SMs at its end.
+#include <algorithm>
+
 #include "dev_kernels.h"
 
 namespace mtgl {
@@ -145,133 +151,214 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, c
     return wrote;
 }
 
-template <bool TEX, bool EYE>
-__global__ void __launch_bounds__(kTileThreads) k_tile(TileArgs A)
+// Without per-fragment lighting the kernel fits 48 registers: ask for 1280 resident
+// threads per SM (5 CTAs of 16x16, 20 of 8x8); with it, 64 registers and 1024 threads. A
+// 32x32 CTA is 1024 threads on its own.
+template <int TS, bool EYE>
+constexpr int tile_min_blocks()
 {
-    __shared__ float4 s_rec[kChunk][kRecWords / 4];
-    __shared__ float4 s_eye[kChunk][kEyeWords / 4];
+    return TS == 32 ? 1 : (EYE ? 1024 : 1280) / (TS * TS);
+}
 
-    const int tile = blockIdx.x;
-    const int tx = tile % A.dims.tiles_x, ty = tile / A.dims.tiles_x;
-    const uint32_t count = A.tile_count[tile];
-    if (count == 0 && A.nclears == 0) return;
+template <int TS, bool TEX, bool EYE>
+__global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(TileArgs A)
+{
+    constexpr int kThreads = TS * TS;
+    constexpr int kWarpsX = TS / 8;  // 8x4-pixel warp blocks per tile row band
+    __shared__ float4 s_rec[kChunk][kRecWords / 4];
+    __shared__ float4 s_eye[EYE ? kChunk : 1][kEyeWords / 4];
+    __shared__ uint32_t s_tile, s_frame;
+
+    if (A.guard && (A.guard[0] > A.records_cap || A.guard[1] > A.pairs_cap)) return;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int px = tx * kTile + (warp & 1) * 8 + (lane & 7);
-    const int py = ty * kTile + (warp >> 1) * 4 + (lane >> 3);
-    const bool in_fb = px < A.dims.width && py < A.dims.height;
-    const size_t pix = (size_t)py * A.dims.width + px;
-
-    // buffers a clear fully covers are never loaded
-    const int bx0 = tx * kTile, by0 = ty * kTile;
-    const int bx1 = min(bx0 + kTile, A.dims.width), by1 = min(by0 + kTile, A.dims.height);
-    bool load_c = true, load_d = true, load_s = true;
-    for (int i = 0; i < A.nclears; i++) {
-        const ClearOp &c = A.clears[i];
-        if (covers_tile(c, GL_COLOR_BUFFER_BIT, bx0, by0, bx1, by1)) load_c = false;
-        if (covers_tile(c, GL_DEPTH_BUFFER_BIT, bx0, by0, bx1, by1)) load_d = false;
-        if (covers_tile(c, GL_STENCIL_BUFFER_BIT, bx0, by0, bx1, by1)) load_s = false;
-    }
-    uint32_t col = 0, st = 0;
-    float dep = 1.0f;
-    if (in_fb) {
-        if (load_c) col = A.color[pix];
-        if (load_d) dep = A.depth[pix];
-        if (load_s) st = A.stencil[pix];
-        for (int i = 0; i < A.nclears; i++) {
-            const ClearOp &c = A.clears[i];
-            if (px >= c.x0 && px < c.x1 && py >= c.y0 && py < c.y1) {
-                if (c.mask & GL_COLOR_BUFFER_BIT) col = c.color;
-                if (c.mask & GL_DEPTH_BUFFER_BIT) dep = c.depth;
-                if (c.mask & GL_STENCIL_BUFFER_BIT) st = c.stencil & 0xFFu;
-            }
-        }
-    }
-
-    const float fpx = (float)px, fpy = (float)py;
-    const uint32_t start = A.tile_start[tile];
-    uint32_t frags = 0;
+    const int ox = (warp % kWarpsX) * 8, oy = (warp / kWarpsX) * 4;  // warp block within the tile
     const bool have_eye = EYE && A.eye_records != nullptr;
-    // this warp's 8x4 pixel block: a staged record is visited only by the warps it overlaps
-    const int wx0 = tx * kTile + (warp & 1) * 8, wy0 = ty * kTile + (warp >> 1) * 4;
-    // hierarchical z: the warp's largest stored depth, refreshed whenever the warp writes depth
-    float wzmax = warp_max_depth(dep, in_fb);
+    uint32_t frags = 0;
 
-    for (uint32_t base = 0; base < count; base += kChunk) {
-        const int n = (int)min((uint32_t)kChunk, count - base);
-        __syncthreads();
-        for (int i = threadIdx.x; i < n * (kRecWords / 4); i += kTileThreads) {
-            const int r = i / (kRecWords / 4), q = i % (kRecWords / 4);
-            const uint32_t idx = __ldg(A.tile_vals + start + base + r);
-            s_rec[r][q] = __ldg(reinterpret_cast<const float4 *>(A.records) + (size_t)idx * (kRecWords / 4) + q);
+    for (uint32_t item = blockIdx.x;;) {
+        if (A.ctas) {
+            if (threadIdx.x == 0) s_tile = atomicAdd(A.queue, 1u);
+            __syncthreads();
+            item = s_tile;
+            __syncthreads();
         }
-        if (have_eye) {
-            for (int i = threadIdx.x; i < n * (kEyeWords / 4); i += kTileThreads) {
-                const int r = i / (kEyeWords / 4), q = i % (kEyeWords / 4);
+        if (item >= A.ntiles) break;
+        const uint32_t tile = A.order ? A.order[item] : item;
+        if (!A.ctas) item = A.ntiles;  // one tile per CTA
+        // the frame owning the tile: last frame whose tile_base <= tile
+        uint32_t f = 0;
+        if (A.nframes > 1) {
+            if (threadIdx.x == 0) {
+                uint32_t lo = 0, hi = A.nframes - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (A.frames[mid].tile_base <= tile) lo = mid;
+                    else hi = mid - 1;
+                }
+                s_frame = lo;
+            }
+            __syncthreads();
+            f = s_frame;
+        }
+        const DevFrame &F = A.frames[f];
+        const uint32_t count = A.tile_count[tile];
+        const ClearOp *clears = A.clears + F.clear_base;
+        const int nclears = (int)F.nclears;
+        if (count == 0 && nclears == 0) continue;
+
+        const uint32_t local = tile - F.tile_base;
+        const int tx = (int)(local % (uint32_t)F.dims.tiles_x), ty = (int)(local / (uint32_t)F.dims.tiles_x);
+        const int wx0 = tx * TS + ox, wy0 = ty * TS + oy;
+        const int px = wx0 + (lane & 7);
+        const int py = wy0 + (lane >> 3);
+        const bool in_fb = px < F.dims.width && py < F.dims.height;
+        const size_t pix = (size_t)py * F.dims.width + px;
+
+        // buffers a clear fully covers are never loaded
+        const int bx0 = tx * TS, by0 = ty * TS;
+        const int bx1 = min(bx0 + TS, F.dims.width), by1 = min(by0 + TS, F.dims.height);
+        bool load_c = true, load_d = true, load_s = true;
+        for (int i = 0; i < nclears; i++) {
+            const ClearOp &c = clears[i];
+            if (covers_tile(c, GL_COLOR_BUFFER_BIT, bx0, by0, bx1, by1)) load_c = false;
+            if (covers_tile(c, GL_DEPTH_BUFFER_BIT, bx0, by0, bx1, by1)) load_d = false;
+            if (covers_tile(c, GL_STENCIL_BUFFER_BIT, bx0, by0, bx1, by1)) load_s = false;
+        }
+        uint32_t col = 0, st = 0;
+        float dep = 1.0f;
+        if (in_fb) {
+            if (load_c) col = F.color[pix];
+            if (load_d) dep = F.depth[pix];
+            if (load_s) st = F.stencil[pix];
+            for (int i = 0; i < nclears; i++) {
+                const ClearOp &c = clears[i];
+                if (px >= c.x0 && px < c.x1 && py >= c.y0 && py < c.y1) {
+                    if (c.mask & GL_COLOR_BUFFER_BIT) col = c.color;
+                    if (c.mask & GL_DEPTH_BUFFER_BIT) dep = c.depth;
+                    if (c.mask & GL_STENCIL_BUFFER_BIT) st = c.stencil & 0xFFu;
+                }
+            }
+        }
+
+        const float fpx = (float)px, fpy = (float)py;
+        const uint32_t start = A.tile_start[tile];
+        // hierarchical z: the warp's largest stored depth, refreshed whenever the warp writes depth
+        float wzmax = warp_max_depth(dep, in_fb);
+
+        for (uint32_t base = 0; base < count; base += kChunk) {
+            const int n = (int)min((uint32_t)kChunk, count - base);
+            __syncthreads();
+            for (int i = threadIdx.x; i < n * (kRecWords / 4); i += kThreads) {
+                const int r = i / (kRecWords / 4), q = i % (kRecWords / 4);
                 const uint32_t idx = __ldg(A.tile_vals + start + base + r);
-                s_eye[r][q] = __ldg(reinterpret_cast<const float4 *>(A.eye_records) + (size_t)idx * (kEyeWords / 4) + q);
+                s_rec[r][q] = __ldg(reinterpret_cast<const float4 *>(A.records) + (size_t)idx * (kRecWords / 4) + q);
+            }
+            if (have_eye) {
+                for (int i = threadIdx.x; i < n * (kEyeWords / 4); i += kThreads) {
+                    const int r = i / (kEyeWords / 4), q = i % (kEyeWords / 4);
+                    const uint32_t idx = __ldg(A.tile_vals + start + base + r);
+                    s_eye[r][q] =
+                        __ldg(reinterpret_cast<const float4 *>(A.eye_records) + (size_t)idx * (kEyeWords / 4) + q);
+                }
+            }
+            __syncthreads();
+
+            // Lane j tests staged record j against the warp: its bbox must meet the warp's block,
+            // and the depth rejection is tried with the warp's max depth as of now. That value is
+            // still an upper bound when record j is reached unless an earlier record of the chunk
+            // may raise depths, so rejection is only taken when none before j can. The set bits,
+            // lowest first, are this warp's records of the chunk in submission order.
+            bool take = false;
+            uint32_t raises = 0;
+            if (lane < n) {
+                const float4 bb = s_rec[lane][1], bb2 = s_rec[lane][2];
+                take = !(__float_as_int(bb2.x) < wx0 || __float_as_int(bb.z) > wx0 + 7 ||
+                         __float_as_int(bb2.y) < wy0 || __float_as_int(bb.w) > wy0 + 3);
+                raises = __float_as_uint(reinterpret_cast<const float *>(s_rec[lane])[R_FLAGS]) & kFlagRaisesDepth;
+            }
+            const uint32_t raise_mask = __ballot_sync(0xffffffffu, raises != 0);
+            if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
+                const float *rl = reinterpret_cast<const float *>(s_rec[lane]);
+                const uint32_t zc = (__float_as_uint(rl[R_FLAGS]) >> 1) & 3u;
+                const float dmin = rl[R_DMIN];
+                if (zc == ZC_NEVER || (zc != ZC_NONE && (dmin > wzmax || (zc == ZC_LESS && dmin == wzmax))))
+                    take = false;
+            }
+            uint32_t todo = __ballot_sync(0xffffffffu, take);
+            while (todo) {
+                const int j = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const float *r = reinterpret_cast<const float *>(s_rec[j]);
+                // warp-uniform rejection: no fragment of this triangle can pass the depth test here
+                const uint32_t zc = (__float_as_uint(r[R_FLAGS]) >> 1) & 3u;
+                if (zc != ZC_NONE) {
+                    const float dmin = r[R_DMIN];
+                    if (zc == ZC_NEVER || dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)) continue;
+                }
+                const bool wrote = shade_pixel<TEX, EYE>(A, r, reinterpret_cast<const float *>(s_eye[EYE ? j : 0]),
+                                                         have_eye, px, py, fpx, fpy, col, dep, st, frags);
+                if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
             }
         }
-        __syncthreads();
 
-        // Lane j tests staged record j against the warp: its bbox must meet the warp's block,
-        // and the depth rejection is tried with the warp's max depth as of now. That value is
-        // still an upper bound when record j is reached unless an earlier record of the chunk
-        // may raise depths, so rejection is only taken when none before j can. The set bits,
-        // lowest first, are this warp's records of the chunk in submission order.
-        bool take = false;
-        uint32_t raises = 0;
-        if (lane < n) {
-            const float4 bb = s_rec[lane][1], bb2 = s_rec[lane][2];
-            take = !(__float_as_int(bb2.x) < wx0 || __float_as_int(bb.z) > wx0 + 7 || __float_as_int(bb2.y) < wy0 ||
-                     __float_as_int(bb.w) > wy0 + 3);
-            raises = __float_as_uint(reinterpret_cast<const float *>(s_rec[lane])[R_FLAGS]) & kFlagRaisesDepth;
+        if (in_fb) {
+            F.color[pix] = col;
+            F.depth[pix] = dep;
+            F.stencil[pix] = (uint8_t)st;
         }
-        const uint32_t raise_mask = __ballot_sync(0xffffffffu, raises != 0);
-        if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
-            const float *rl = reinterpret_cast<const float *>(s_rec[lane]);
-            const uint32_t zc = (__float_as_uint(rl[R_FLAGS]) >> 1) & 3u;
-            const float dmin = rl[R_DMIN];
-            if (zc == ZC_NEVER || (zc != ZC_NONE && (dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)))) take = false;
-        }
-        uint32_t todo = __ballot_sync(0xffffffffu, take);
-        while (todo) {
-            const int j = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const float *r = reinterpret_cast<const float *>(s_rec[j]);
-            // warp-uniform rejection: no fragment of this triangle can pass the depth test here
-            const uint32_t zc = (__float_as_uint(r[R_FLAGS]) >> 1) & 3u;
-            if (zc != ZC_NONE) {
-                const float dmin = r[R_DMIN];
-                if (zc == ZC_NEVER || dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)) continue;
-            }
-            const bool wrote = shade_pixel<TEX, EYE>(A, r, reinterpret_cast<const float *>(s_eye[j]), have_eye, px,
-                                                     py, fpx, fpy, col, dep, st, frags);
-            if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
-        }
-    }
-
-    if (in_fb) {
-        A.color[pix] = col;
-        A.depth[pix] = dep;
-        A.stencil[pix] = (uint8_t)st;
     }
     if (A.fragments) {
-        uint32_t f = __reduce_add_sync(0xffffffffu, frags);
-        if (lane == 0 && f) atomicAdd(A.fragments, (unsigned long long)f);
+        const uint32_t fw = __reduce_add_sync(0xffffffffu, frags);
+        if (lane == 0 && fw) atomicAdd(A.fragments, (unsigned long long)fw);
+    }
+}
+
+template <int TS, bool TEX, bool EYE>
+struct TileVariant {
+    static int occupancy()
+    {
+        static int occ = -1;
+        if (occ < 0) {
+            int n = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tile<TS, TEX, EYE>, TS * TS, 0) != cudaSuccess)
+                n = 1;
+            occ = n > 0 ? n : 1;
+        }
+        return occ;
+    }
+    static void launch(const TileArgs &a, cudaStream_t s)
+    {
+        const unsigned grid = a.ctas ? (unsigned)std::min<uint32_t>((uint32_t)a.ctas, a.ntiles) : a.ntiles;
+        k_tile<TS, TEX, EYE><<<grid, TS * TS, 0, s>>>(a);
+    }
+};
+
+template <int TS>
+int dispatch_tile(const TileArgs &a, cudaStream_t s, bool occ_only)
+{
+    const bool eye = a.eye_records != nullptr;
+    if (a.any_texture && eye) return occ_only ? TileVariant<TS, true, true>::occupancy() : (TileVariant<TS, true, true>::launch(a, s), 1);
+    if (a.any_texture) return occ_only ? TileVariant<TS, true, false>::occupancy() : (TileVariant<TS, true, false>::launch(a, s), 1);
+    if (eye) return occ_only ? TileVariant<TS, false, true>::occupancy() : (TileVariant<TS, false, true>::launch(a, s), 1);
+    return occ_only ? TileVariant<TS, false, false>::occupancy() : (TileVariant<TS, false, false>::launch(a, s), 1);
+}
+
+int dispatch_tile_size(const TileArgs &a, cudaStream_t s, bool occ_only)
+{
+    switch (a.tile_shift) {
+    case 3: return dispatch_tile<8>(a, s, occ_only);
+    case 5: return dispatch_tile<32>(a, s, occ_only);
+    default: return dispatch_tile<16>(a, s, occ_only);
     }
 }
 
 int launch_tile(const TileArgs &a, cudaStream_t s)
 {
-    const int ntiles = a.dims.tiles_x * a.dims.tiles_y;
-    if (ntiles == 0) return 0;
-    const bool eye = a.eye_records != nullptr;
-    if (a.any_texture && eye) k_tile<true, true><<<ntiles, kTileThreads, 0, s>>>(a);
-    else if (a.any_texture) k_tile<true, false><<<ntiles, kTileThreads, 0, s>>>(a);
-    else if (eye) k_tile<false, true><<<ntiles, kTileThreads, 0, s>>>(a);
-    else k_tile<false, false><<<ntiles, kTileThreads, 0, s>>>(a);
-    return 1;
+    if (a.ntiles == 0) return 0;
+    return dispatch_tile_size(a, s, false);
 }
+
+int tile_occupancy(const TileArgs &a) { return dispatch_tile_size(a, nullptr, true); }
 
 }  // namespace mtgl

@@ -17,8 +17,9 @@ namespace mtgl {
 
 // ------------------------------------------------------------------ layout constants
 
-constexpr int kTile = 16;            // tile edge in pixels (one CTA per tile)
-constexpr int kTileThreads = kTile * kTile;
+constexpr int kTileShiftMin = 3;     // tile edges of 8, 16 or 32 pixels (one CTA per tile)
+constexpr int kTileShiftMax = 5;
+constexpr int kTileShiftPlain = 4;   // 16x16 tiles for single-frame passes
 constexpr int kRecWords = 56;        // words per triangle record (224 bytes)
 constexpr int kEyeWords = 20;        // words per triangle eye-space record (per-fragment lighting)
 
@@ -39,7 +40,7 @@ enum RecField {
     R_RASTER = 47,                            // uint32 raster-state index
     R_FLAGS = 48,                             // bit 0 back facing; bits 1-2 depth rejection mode
     R_EA0 = 49, R_EB0, R_EA1, R_EB1, R_EA2, R_EB2,  // per-edge (by-ay), (bx-ax) of edge_function
-    R_PAD = 55
+    R_FRAME = 55                              // uint32 frame index within the pass's frame table
 };
 
 // Depth rejection modes (R_FLAGS bits 1-2). A warp skips a triangle when no fragment of it
@@ -98,7 +99,7 @@ struct DevRaster {
     int32_t default_depth_range;
     int32_t needs_eye;     // per-fragment lighting reads eye-space interpolants
     int32_t depth_rejection;  // MTGL_OPT_DEPTH_REJECTION of the context at enqueue
-    int32_t pad_;
+    uint32_t frame;           // index of the frame (framebuffer) the draw renders into
 };
 
 struct ClearOp {
@@ -112,6 +113,19 @@ struct ClearOp {
 struct FrameDims {
     int32_t width, height;
     int32_t tiles_x, tiles_y;
+};
+
+// One framebuffer of a pass. A single-context pass has one frame; a batch has one per
+// context. Tiles of all frames are numbered consecutively: frame f owns global tiles
+// [tile_base, tile_base + tiles_x * tiles_y). Its clears are clears[clear_base .. +nclears).
+struct DevFrame {
+    uint32_t *color;
+    float *depth;
+    uint8_t *stencil;
+    FrameDims dims;
+    uint32_t tile_base;
+    uint32_t clear_base, nclears;
+    uint32_t pad_;
 };
 
 // ------------------------------------------------------------------ scalar helpers

@@ -45,7 +45,8 @@ def _parse_header(path=GL_HEADER):
     for name, val in re.findall(r"^#define\s+(GL_\w+)\s+(0x[0-9A-Fa-f]+|\d+)", text, re.M):
         enums[name] = int(val, 0)
     protos = {}
-    for ret, name, args in re.findall(r"^\s*(const GLubyte \*|\w+)\s+(gl\w+)\(([^)]*)\);", text, re.M):
+    for ret, name, args in re.findall(r"^\s*(const GLubyte \*\s*|\w+\s+)(gl\w+)\(([^)]*)\);", text, re.M):
+        ret = ret.strip()
         if ret.startswith("const GLubyte"):
             restype = ctypes.c_char_p
         else:
@@ -80,6 +81,39 @@ def _ptr(x):
     return int(x)
 
 
+class Stats(ctypes.Structure):
+    """mtgl_stats (include/mytinygl/mtgl_dev.h)"""
+    _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "input_triangles", "setup_triangles", "bin_entries",
+                                               "fragments", "passes", "kernel_launches")]
+
+
+class BatchConfig(ctypes.Structure):
+    """mtgl_batch_config (include/mytinygl/mtgl_dev.h); zero fields take the tuned defaults."""
+    _fields_ = [("tile_size", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("record_factor", ctypes.c_float),
+                ("pair_factor", ctypes.c_float), ("use_graph", ctypes.c_int32), ("order_by_cost", ctypes.c_int32)]
+
+
+class BatchStats(ctypes.Structure):
+    """mtgl_batch_stats (include/mytinygl/mtgl_dev.h)"""
+    _fields_ = [(n, ctypes.c_uint64) for n in ("batches", "frames", "input_triangles", "setup_triangles",
+                                               "bin_entries", "fragments", "graph_captures", "graph_replays",
+                                               "overflow_reruns", "kernel_launches")] + \
+               [("record_capacity", ctypes.c_uint32), ("pair_capacity", ctypes.c_uint32),
+                ("tile_size", ctypes.c_int32), ("ctas", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Timings(ctypes.Structure):
+    """mtgl_timings (include/mytinygl/mtgl_dev.h)"""
+    _fields_ = [("vertex_ms", ctypes.c_double), ("setup_ms", ctypes.c_double), ("bin_ms", ctypes.c_double),
+                ("tile_ms", ctypes.c_double), ("passes", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class GLLibrary:
     """One loaded GL implementation (a shared library exporting include/GL/gl.h)."""
 
@@ -105,6 +139,38 @@ class GLLibrary:
         L.mtgl_finish.argtypes = [ctypes.c_void_p]
         L.mtgl_backend_name.restype = ctypes.c_char_p
         L.mtgl_backend_name.argtypes = []
+        L.mtgl_get_stats.restype = ctypes.c_int
+        L.mtgl_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+        self.has_player = hasattr(L, "mtgl_play")  # the reference build has none
+        if self.has_player:
+            L.mtgl_play.restype = ctypes.c_int
+            L.mtgl_play.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+            L.mtgl_play_many.restype = ctypes.c_int
+            L.mtgl_play_many.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                         ctypes.POINTER(ctypes.c_size_t), ctypes.c_int32]
+        self.has_batches = hasattr(L, "mtgl_dev_batch_create")  # the reference build has none
+        if self.has_batches:
+            self._bind_batches(L)
+
+    @staticmethod
+    def _bind_batches(L):
+        L.mtgl_dev_batch_defaults.restype = None
+        L.mtgl_dev_batch_defaults.argtypes = [ctypes.POINTER(BatchConfig)]
+        L.mtgl_dev_batch_create.restype = ctypes.c_int
+        L.mtgl_dev_batch_create.argtypes = [ctypes.POINTER(BatchConfig), ctypes.POINTER(ctypes.c_void_p)]
+        for n in ("mtgl_dev_batch_destroy", "mtgl_dev_batch_wait", "mtgl_dev_batch_reset_stats"):
+            getattr(L, n).restype = ctypes.c_int
+            getattr(L, n).argtypes = [ctypes.c_void_p]
+        L.mtgl_dev_batch_stats.restype = ctypes.c_int
+        L.mtgl_dev_batch_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchStats)]
+        L.mtgl_dev_batch_profile.restype = ctypes.c_int
+        L.mtgl_dev_batch_profile.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.mtgl_dev_batch_timings.restype = ctypes.c_int
+        L.mtgl_dev_batch_timings.argtypes = [ctypes.c_void_p, ctypes.POINTER(Timings)]
+        L.mtgl_dev_batch_stream.restype = ctypes.c_void_p
+        L.mtgl_dev_batch_stream.argtypes = [ctypes.c_void_p]
+        L.mtgl_batch_render.restype = ctypes.c_int
+        L.mtgl_batch_render.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]
 
     @property
     def backend(self) -> str:
@@ -112,6 +178,105 @@ class GLLibrary:
 
     def context(self, width: int, height: int) -> "GLContext":
         return GLContext(self, width, height)
+
+    def play(self, ctx: "GLContext", stream: bytes):
+        """Replay an encoded command stream (mytinygl_gb300.gen_play.encode) onto ctx."""
+        st = self.lib.mtgl_play(ctx.handle, stream, len(stream))
+        if st != 0:
+            raise RuntimeError(f"mtgl_play failed with status {st}")
+
+    def play_many(self, contexts, streams):
+        """Replay streams[i] onto contexts[i] for every i with one native call."""
+        PreparedStreams(self, contexts, streams).play()
+
+
+    def batch(self, **config) -> "Batch":
+        """A batch executor; keyword arguments override fields of mtgl_batch_config."""
+        return Batch(self, **config)
+
+
+class PreparedStreams:
+    """Command streams bound to their contexts once, for replaying with one native call."""
+
+    def __init__(self, glib: GLLibrary, contexts, streams):
+        n = len(contexts)
+        if len(streams) != n:
+            raise ValueError("one stream per context")
+        self.glib = glib
+        self.contexts = list(contexts)
+        self._bufs = [ctypes.create_string_buffer(bytes(s), len(s)) for s in streams]
+        self._ctxs = (ctypes.c_void_p * n)(*[c.handle for c in contexts])
+        self._ptrs = (ctypes.c_void_p * n)(*[ctypes.addressof(b) for b in self._bufs])
+        self._sizes = (ctypes.c_size_t * n)(*[len(s) for s in streams])
+        self.n = n
+
+    def play(self):
+        st = self.glib.lib.mtgl_play_many(self._ctxs, self._ptrs, self._sizes, self.n)
+        if st != 0:
+            raise RuntimeError(f"mtgl_play_many failed with status {st}")
+
+
+class Batch:
+    """mtgl_batch: renders many contexts' pending frames in one pipeline run."""
+
+    def __init__(self, glib: GLLibrary, **config):
+        self.glib = glib
+        cfg = BatchConfig()
+        glib.lib.mtgl_dev_batch_defaults(ctypes.byref(cfg))
+        for k, v in config.items():
+            setattr(cfg, k, v)
+        self.config = cfg
+        h = ctypes.c_void_p()
+        st = glib.lib.mtgl_dev_batch_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            raise RuntimeError(f"mtgl_dev_batch_create failed with status {st}")
+        self.handle = h.value
+
+    def render(self, contexts):
+        arr = (ctypes.c_void_p * len(contexts))(*[c.handle for c in contexts])
+        st = self.glib.lib.mtgl_batch_render(self.handle, arr, len(contexts))
+        if st != 0:
+            raise RuntimeError(f"mtgl_batch_render failed with status {st}")
+
+    def wait(self):
+        st = self.glib.lib.mtgl_dev_batch_wait(self.handle)
+        if st != 0:
+            raise RuntimeError(f"mtgl_dev_batch_wait failed with status {st}")
+
+    def stats(self) -> dict:
+        s = BatchStats()
+        st = self.glib.lib.mtgl_dev_batch_stats(self.handle, ctypes.byref(s))
+        if st != 0:
+            raise RuntimeError(f"mtgl_dev_batch_stats failed with status {st}")
+        return s.as_dict()
+
+    def reset_stats(self):
+        self.glib.lib.mtgl_dev_batch_reset_stats(self.handle)
+
+    def profile(self, enable: bool):
+        self.glib.lib.mtgl_dev_batch_profile(self.handle, 1 if enable else 0)
+
+    def timings(self) -> dict:
+        t = Timings()
+        st = self.glib.lib.mtgl_dev_batch_timings(self.handle, ctypes.byref(t))
+        if st != 0:
+            raise RuntimeError(f"mtgl_dev_batch_timings failed with status {st}")
+        return t.as_dict()
+
+    @property
+    def stream(self) -> int:
+        return self.glib.lib.mtgl_dev_batch_stream(self.handle) or 0
+
+    def destroy(self):
+        if self.handle:
+            self.glib.lib.mtgl_dev_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 class GLContext:
@@ -178,6 +343,14 @@ class GLContext:
 
     def forget_arrays(self):
         self._keep = []
+
+    def stats(self) -> dict:
+        """mtgl_get_stats (synchronises)"""
+        s = Stats()
+        st = self.glib.lib.mtgl_get_stats(self.handle, ctypes.byref(s))
+        if st != 0:
+            raise RuntimeError(f"mtgl_get_stats failed with status {st}")
+        return {n: getattr(s, n) for n, _ in Stats._fields_}
 
 
 _lib_cache: dict = {}

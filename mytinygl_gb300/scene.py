@@ -38,6 +38,12 @@ class Scene:
         for name, args in self.cmds[start:stop]:
             ctx.call(name, *args)
 
+    def stream(self, start=0, stop=None) -> bytes:
+        """The calls [start, stop) as a native command stream (mtgl_play). Arrays are passed
+        by address, so the scene must outlive every replay of the stream."""
+        from .gen_play import encode
+        return encode(self.cmds[start:stop])
+
     # ---- serialisation -------------------------------------------------------------
     def to_bytes(self) -> bytes:
         arrays = {}

@@ -75,23 +75,40 @@ def _vbo(s: Scene, target, data: np.ndarray, buf_id: int):
     s.glBufferData(target, int(data.nbytes), data, G.GL_STATIC_DRAW)
 
 
-def sphere_scene(width=800, height=600, seed=0, use_vbo=True, near=0.1, far=100.0, stacks=32, slices=32):
+def sphere_uv(stacks, slices):
+    """Texture coordinates (slice / slices, stack / stacks) per vertex of uv_sphere."""
+    i, j = np.meshgrid(np.arange(stacks + 1), np.arange(slices + 1), indexing="ij")
+    return np.stack([j / slices, i / stacks], axis=-1).reshape(-1, 2).astype(np.float32)
+
+
+def sphere_scene(width=800, height=600, seed=0, use_vbo=True, near=0.1, far=100.0, stacks=32, slices=32,
+                 light=(0.0, 0.0, 1.0), tex_size=0):
     """Plain single frame: 800x600 RGBA8 + float depth cleared to black, UV sphere r=1 of
     32 stacks x 32 slices (1,984 triangles), gluPerspective(60, w/h, 0.1, 100) at z=-3,
     Euler angles U[0, 2pi) from `seed`, GL_LIGHT0 directional white at (0,0,1,0) set before
-    the model rotation, Gouraud shading, GL_LESS, back-face culling, no texture."""
+    the model rotation, Gouraud shading, GL_LESS, back-face culling, no texture. With
+    tex_size > 0 the sphere also carries a tex_size^2 noise texture (seeded by `seed`,
+    GL_LINEAR_MIPMAP_LINEAR, GL_MODULATE) mapped by (slice, stack)."""
     rng = np.random.default_rng(seed)
     ang = rng.uniform(0.0, 2 * math.pi, 3)
     pos, nrm, idx = uv_sphere(stacks, slices)
     s = Scene("sphere", width, height)
+    if tex_size:
+        s.glGenTextures(1, np.zeros(1, np.uint32))
+        s.glBindTexture(G.GL_TEXTURE_2D, 1)
+        s.glTexImage2D(G.GL_TEXTURE_2D, 0, G.GL_RGBA, tex_size, tex_size, 0, G.GL_RGBA, G.GL_UNSIGNED_BYTE,
+                       np.ascontiguousarray(noise_texture(tex_size, seed)))
+    uv = sphere_uv(stacks, slices)
     if use_vbo:
-        # resident inputs, uploaded before the frame: one interleaved position+normal buffer
-        # (24-byte records; the array-buffer binding is read at draw time, so one buffer
-        # serves both pointers) and an element buffer
+        # resident inputs, uploaded before the frame: one interleaved position+normal(+uv)
+        # buffer (the array-buffer binding is read at draw time, so one buffer serves every
+        # pointer) and an element buffer
         s.glGenBuffers(2, np.zeros(2, np.uint32))
-        inter = np.ascontiguousarray(np.concatenate([pos, nrm], axis=1).astype(np.float32))
+        cols = [pos, nrm] + ([uv] if tex_size else [])
+        inter = np.ascontiguousarray(np.concatenate(cols, axis=1).astype(np.float32))
         _vbo(s, G.GL_ARRAY_BUFFER, inter, 1)
         _vbo(s, G.GL_ELEMENT_ARRAY_BUFFER, idx, 2)
+    stride = 32 if tex_size else 24
     s.glViewport(0, 0, width, height)
     s.glClearColor(0.0, 0.0, 0.0, 1.0)
     # ---- frame
@@ -101,7 +118,7 @@ def sphere_scene(width=800, height=600, seed=0, use_vbo=True, near=0.1, far=100.
     s.glFrustum(*frustum_params(60.0, width / height, near, far))
     s.glMatrixMode(G.GL_MODELVIEW)
     s.glLoadIdentity()
-    s.glLightfv(G.GL_LIGHT0, G.GL_POSITION, np.array([0, 0, 1, 0], np.float32))
+    s.glLightfv(G.GL_LIGHT0, G.GL_POSITION, np.array([*light, 0], np.float32))
     s.glLightfv(G.GL_LIGHT0, G.GL_DIFFUSE, np.array([1, 1, 1, 1], np.float32))
     s.glEnable(G.GL_LIGHTING)
     s.glEnable(G.GL_LIGHT0)
@@ -112,20 +129,33 @@ def sphere_scene(width=800, height=600, seed=0, use_vbo=True, near=0.1, far=100.
     s.glCullFace(G.GL_BACK)
     s.glTranslatef(0.0, 0.0, -3.0)
     s.glMultMatrixf(euler_matrix(*ang))
+    if tex_size:
+        s.glBindTexture(G.GL_TEXTURE_2D, 1)
+        s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MIN_FILTER, G.GL_LINEAR_MIPMAP_LINEAR)
+        s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MAG_FILTER, G.GL_LINEAR)
+        s.glTexEnvi(G.GL_TEXTURE_ENV, G.GL_TEXTURE_ENV_MODE, G.GL_MODULATE)
+        s.glEnable(G.GL_TEXTURE_2D)
+        s.glEnableClientState(G.GL_TEXTURE_COORD_ARRAY)
     s.glEnableClientState(G.GL_VERTEX_ARRAY)
     s.glEnableClientState(G.GL_NORMAL_ARRAY)
     if use_vbo:
         s.glBindBuffer(G.GL_ARRAY_BUFFER, 1)
         s.glBindBuffer(G.GL_ELEMENT_ARRAY_BUFFER, 2)
-        s.glVertexPointer(3, G.GL_FLOAT, 24, 0)
-        s.glNormalPointer(G.GL_FLOAT, 24, 12)
+        s.glVertexPointer(3, G.GL_FLOAT, stride, 0)
+        s.glNormalPointer(G.GL_FLOAT, stride, 12)
+        if tex_size:
+            s.glTexCoordPointer(2, G.GL_FLOAT, stride, 24)
         s.glDrawElements(G.GL_TRIANGLES, int(idx.size), G.GL_UNSIGNED_INT, 0)
     else:
         s.glVertexPointer(3, G.GL_FLOAT, 0, pos)
         s.glNormalPointer(G.GL_FLOAT, 0, nrm)
+        if tex_size:
+            s.glTexCoordPointer(2, G.GL_FLOAT, 0, uv)
         s.glDrawElements(G.GL_TRIANGLES, int(idx.size), G.GL_UNSIGNED_INT, idx)
     s.glDisableClientState(G.GL_VERTEX_ARRAY)
     s.glDisableClientState(G.GL_NORMAL_ARRAY)
+    if tex_size:
+        s.glDisableClientState(G.GL_TEXTURE_COORD_ARRAY)
     return s
 
 
@@ -138,7 +168,8 @@ TEXTURED_SPREAD = 0.33  # per-vertex offset U[-s, s]: ~30 % of the triangles str
 
 
 def textured_scene(width=1920, height=1080, ntri=100_000, seed=1, tex_size=512, use_vbo=True,
-                   spread=TEXTURED_SPREAD, fog=True, lights=8, min_filter=G.GL_LINEAR_MIPMAP_LINEAR):
+                   spread=TEXTURED_SPREAD, fog=True, lights=8, min_filter=G.GL_LINEAR_MIPMAP_LINEAR,
+                   rotate_z=0.0):
     """Textured with clipping and fog: identity modelview/projection; triangle centres
     U[-1.5, 1.5]^3 in clip space with per-vertex offsets U[-s, s]^3; per-vertex RGBA8 colour
     U[0,255], uv U[0,4) with GL_REPEAT, normals U[-1,1]^3; a tex_size^2 RGBA8 noise texture
@@ -176,6 +207,8 @@ def textured_scene(width=1920, height=1080, ntri=100_000, seed=1, tex_size=512, 
     s.glLoadIdentity()
     s.glMatrixMode(G.GL_MODELVIEW)
     s.glLoadIdentity()
+    if rotate_z:
+        s.glMultMatrixf(euler_matrix(0.0, 0.0, rotate_z))
     s.glBindTexture(G.GL_TEXTURE_2D, 1)
     s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MIN_FILTER, min_filter)
     s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MAG_FILTER, G.GL_LINEAR)
@@ -284,6 +317,53 @@ def rop_scene(width=1920, height=1080, ntri=1_000_000, seed=2, median_area=20.0,
     s.glDisableClientState(G.GL_VERTEX_ARRAY)
     s.glDisableClientState(G.GL_COLOR_ARRAY)
     return s
+
+
+def _log_uniform(rng, lo, hi):
+    return math.exp(rng.uniform(math.log(lo), math.log(hi)))
+
+
+def uneven_frame(index, seed=3, min_side=64, max_side=1024, min_tri=100, max_tri=200_000, tex_size=256,
+                 use_vbo=True):
+    """Frame `index` of the uneven batch: width and height log-uniform in [min_side, max_side],
+    a triangle count log-uniform in [min_tri, max_tri], drawn with probability 1/2 like the
+    sphere frame (a UV sphere tessellated to about that many triangles, its own rotation and
+    directional light) or like the textured frame (that many clip-straddling triangles, its
+    own rotation about z and 8 point lights); each frame has its own tex_size^2 mipmapped
+    noise texture. Geometry sits in buffer objects uploaded before the frame (use_vbo) or
+    in client arrays read at every draw."""
+    rng = np.random.default_rng([seed, index])
+    w = int(round(_log_uniform(rng, min_side, max_side)))
+    h = int(round(_log_uniform(rng, min_side, max_side)))
+    ntri = int(round(_log_uniform(rng, min_tri, max_tri)))
+    fseed = int(rng.integers(0, 2**31 - 1))
+    if rng.uniform() < 0.5:
+        n = max(3, int(round(0.5 + math.sqrt(0.25 + ntri / 2.0))))  # 2 n (n - 1) triangles
+        light = rng.normal(size=3)
+        light = tuple(float(v) for v in (light / np.linalg.norm(light)).astype(np.float32))
+        s = sphere_scene(w, h, seed=fseed, stacks=n, slices=n, light=light, tex_size=tex_size, use_vbo=use_vbo)
+        s.name = f"uneven{index}_sphere"
+    else:
+        s = textured_scene(w, h, ntri=ntri, seed=fseed, tex_size=tex_size,
+                           rotate_z=float(rng.uniform(0.0, 2 * math.pi)), use_vbo=use_vbo)
+        s.name = f"uneven{index}_textured"
+    return s
+
+
+def uneven_batch(nframes=256, seed=3, **kw):
+    """The batched uneven-frames workload: `nframes` independent frames (uneven_frame)."""
+    return [uneven_frame(i, seed=seed, **kw) for i in range(nframes)]
+
+
+def scene_triangles(scene: Scene) -> int:
+    """Input triangles of a scene's draw calls (GL_TRIANGLES arrays and elements)."""
+    n = 0
+    for name, args in scene.cmds:
+        if name == "glDrawArrays" and args[0] == G.GL_TRIANGLES:
+            n += int(args[2]) // 3
+        elif name == "glDrawElements" and args[0] == G.GL_TRIANGLES:
+            n += int(args[1]) // 3
+    return n
 
 
 HEADLINE = {

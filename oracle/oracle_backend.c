@@ -1392,3 +1392,95 @@ int mtgl_dev_set_option(mtgl_dev *d, int option, int value)
     (void)value;
     return option == MTGL_OPT_DEPTH_REJECTION ? MTGL_OK : MTGL_ERR_INVALID;
 }
+
+/* ------------------------------------------------------------------ batches
+ * The oracle renders every packet as it arrives, so by the time contexts are handed to a
+ * batch their frames are complete: a batch only counts what it is given. */
+struct mtgl_batch {
+    mtgl_batch_config cfg;
+    mtgl_batch_stats stats;
+};
+
+void mtgl_dev_batch_defaults(mtgl_batch_config *cfg)
+{
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->tile_size = 16;
+    cfg->record_factor = 1.5f;
+    cfg->pair_factor = 8.0f;
+    cfg->use_graph = 1;
+    cfg->order_by_cost = 1;
+}
+
+int mtgl_dev_batch_create(const mtgl_batch_config *cfg, mtgl_batch **out)
+{
+    mtgl_batch *b;
+    if (!out) return MTGL_ERR_INVALID;
+    b = (mtgl_batch *)calloc(1, sizeof(*b));
+    if (!b) return MTGL_ERR_OOM;
+    mtgl_dev_batch_defaults(&b->cfg);
+    if (cfg && cfg->tile_size) b->cfg.tile_size = cfg->tile_size;
+    b->stats.tile_size = b->cfg.tile_size;
+    *out = b;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_destroy(mtgl_batch *b)
+{
+    free(b);
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
+{
+    if (!b || n < 0 || (n > 0 && !devs)) return MTGL_ERR_INVALID;
+    b->stats.batches++;
+    b->stats.frames += (uint64_t)n;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_wait(mtgl_batch *b) { return b ? MTGL_OK : MTGL_ERR_INVALID; }
+
+int mtgl_dev_batch_stats(mtgl_batch *b, mtgl_batch_stats *out)
+{
+    if (!b || !out) return MTGL_ERR_INVALID;
+    *out = b->stats;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_reset_stats(mtgl_batch *b)
+{
+    int32_t ts;
+    if (!b) return MTGL_ERR_INVALID;
+    ts = b->stats.tile_size;
+    memset(&b->stats, 0, sizeof(b->stats));
+    b->stats.tile_size = ts;
+    return MTGL_OK;
+}
+
+void *mtgl_dev_batch_stream(mtgl_batch *b)
+{
+    (void)b;
+    return NULL;
+}
+
+int mtgl_dev_batch_profile(mtgl_batch *b, int enable)
+{
+    (void)enable;
+    return b ? MTGL_OK : MTGL_ERR_INVALID;
+}
+
+int mtgl_dev_batch_timings(mtgl_batch *b, mtgl_timings *out)
+{
+    if (!b || !out) return MTGL_ERR_INVALID;
+    memset(out, 0, sizeof(*out));
+    return MTGL_OK;
+}
+
+int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n)
+{
+    if (!b || n < 0 || (n > 0 && !ctxs)) return MTGL_ERR_INVALID;
+    b->stats.batches++;
+    b->stats.frames += (uint64_t)n;
+    return MTGL_OK;
+}

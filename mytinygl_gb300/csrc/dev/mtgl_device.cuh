@@ -135,7 +135,18 @@ __device__ __forceinline__ int32_t x86_f2i(float f)
     return (f >= -2147483648.0f && f < 2147483648.0f) ? (int32_t)f : INT32_MIN;
 }
 
-__device__ __forceinline__ float u8f(uint32_t v) { return (float)v / 255.0f; }
+// (float)v / 255.0f (graphics.h:350-357, textures.c:294-307) for v in [0, 255], without a
+// division: the product with the rounded reciprocal, corrected once by its exact residual
+// (Markstein's FMA correction). The result equals the IEEE quotient for every byte value
+// (checked exhaustively with exact rational arithmetic in tests/test_arith.py).
+__device__ __forceinline__ float u8f(uint32_t v)
+{
+    const float x = (float)v;
+    const float r = 0x1.010102p-8f;  // 1.0f / 255.0f rounded to float
+    const float q = x * r;
+    const float e = __fmaf_rn(-q, 255.0f, x);
+    return __fmaf_rn(e, r, q);
+}
 
 // color_to_rgba32 (graphics.h:337-348)
 __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a)
@@ -280,12 +291,25 @@ struct TexView {
     int32_t w, h;
 };
 
-__device__ __forceinline__ uint32_t texel_wrapped(const TexView &t, int32_t ws, int32_t wt, int32_t x, int32_t y)
+// get_texel_wrapped's coordinate rule (textures.c:272-291): GL_REPEAT is ((x % n) + n) % n,
+// anything else clamps to [0, n-1]. For a power-of-two n the REPEAT result is x & (n - 1)
+// (the same value for every int x, negative ones included), which avoids two integer
+// divisions per coordinate.
+__device__ __forceinline__ int32_t wrap_coord(int32_t x, int32_t n, bool repeat)
 {
-    if (ws == GL_REPEAT) x = ((x % t.w) + t.w) % t.w;
-    else { if (x < 0) x = 0; else if (x >= t.w) x = t.w - 1; }
-    if (wt == GL_REPEAT) y = ((y % t.h) + t.h) % t.h;
-    else { if (y < 0) y = 0; else if (y >= t.h) y = t.h - 1; }
+    if (repeat) return (n & (n - 1)) == 0 ? (x & (n - 1)) : ((x % n) + n) % n;
+    return x < 0 ? 0 : (x >= n ? n - 1 : x);
+}
+
+// wrap_coord(x + 1) from xa = wrap_coord(x): under GL_REPEAT it is (xa + 1) mod n
+__device__ __forceinline__ int32_t wrap_next(int32_t xa, int32_t x, int32_t n, bool repeat)
+{
+    if (repeat) return xa + 1 == n ? 0 : xa + 1;
+    return wrap_coord(x + 1, n, false);
+}
+
+__device__ __forceinline__ uint32_t texel_at(const TexView &t, int32_t x, int32_t y)
+{
     return __ldg(t.px + (size_t)y * t.w + x);
 }
 
@@ -296,10 +320,13 @@ __device__ __forceinline__ uint32_t sample_level(const TexView &t, int32_t ws, i
     if (linear) {
         int32_t x0 = x86_f2i(floorf(tx)), y0 = x86_f2i(floorf(ty));
         float fx = tx - (float)x0, fy = ty - (float)y0;
-        float4 c00 = unpack_rgba(texel_wrapped(t, ws, wt, x0, y0));
-        float4 c10 = unpack_rgba(texel_wrapped(t, ws, wt, x0 + 1, y0));
-        float4 c01 = unpack_rgba(texel_wrapped(t, ws, wt, x0, y0 + 1));
-        float4 c11 = unpack_rgba(texel_wrapped(t, ws, wt, x0 + 1, y0 + 1));
+        const bool rs = ws == GL_REPEAT, rt = wt == GL_REPEAT;
+        const int32_t xa = wrap_coord(x0, t.w, rs), xb = wrap_next(xa, x0, t.w, rs);
+        const int32_t ya = wrap_coord(y0, t.h, rt), yb = wrap_next(ya, y0, t.h, rt);
+        float4 c00 = unpack_rgba(texel_at(t, xa, ya));
+        float4 c10 = unpack_rgba(texel_at(t, xb, ya));
+        float4 c01 = unpack_rgba(texel_at(t, xa, yb));
+        float4 c11 = unpack_rgba(texel_at(t, xb, yb));
         float4 top = lerp_col(c00, c10, fx);
         float4 bot = lerp_col(c01, c11, fx);
         float4 r = lerp_col(top, bot, fy);

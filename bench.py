@@ -56,6 +56,11 @@ WORKLOADS["batch"] = dict(builder=None, full_tris=None, name="uneven_batch_256_f
                           desc=("256 independent frames, sides log-uniform 64-1024, triangles log-uniform "
                                 "100-200k, each a lit UV sphere or a clip-straddling textured frame (p=1/2) "
                                 "with its own modelview, lights and 256^2 mipmapped texture; seed 3"))
+WORKLOADS["serve"] = dict(builder=None, full_tris=None, name="serve_32_scenes_poisson_2000",
+                          desc=("serving loop: 32 resident scenes (1k-500k triangles like the textured frame, "
+                                "256^2-2048^2 mipmapped textures), Poisson arrivals at 2,000 req/s, resolution "
+                                "uniform over 256^2, 512^2, 1280x720, 1920x1080, modelview from the request "
+                                "seed, 40 GiB framebuffer + pipeline-scratch budget"))
 REC_BYTES = 224  # triangle record written by the setup kernel, read by the tile kernel
 BATCH_FRAMES = 256
 
@@ -546,6 +551,109 @@ def run_batch(args, spec):
     return out if rank == 0 else None
 
 
+def _serve_requests(trace, base, outs=None):
+    reqs = (G.Request * len(trace))()
+    for i, (t, sc, w, h, mv) in enumerate(trace):
+        r = reqs[i]
+        r.scene, r.width, r.height = sc, w, h
+        r.modelview[:] = [float(v) for v in mv]
+        r.arrival = base + t
+        r.color = outs(i, w, h) if outs else None
+    return reqs
+
+
+def _latency_summary(reqs):
+    lat = np.array([r.finished - r.arrival for r in reqs if r.status == 0]) * 1e3
+    ok = [r for r in reqs if r.status == 0]
+    span = max(r.finished for r in ok) - min(r.arrival for r in ok)
+    return {"p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "mean_ms": round(float(lat.mean()), 3), "max_ms": round(float(lat.max()), 3),
+            "completed": len(ok), "failed": len(reqs) - len(ok),
+            "frames_per_s": round(len(ok) / span, 2),
+            "mean_batch": round(float(np.mean([r.batch_size for r in ok])), 2)}
+
+
+def run_serve(args, spec):
+    """The serving workload: a Poisson trace replayed against the C serving loop.
+
+    value: frames/s completed over the trace (first arrival to last completion), frames
+    left in device framebuffers; latency = completion - arrival on the server clock.
+    e2e: a shorter trace at the same rate with every frame read back into page-locked
+    host buffers (a ring larger than the requests that can be in flight)."""
+    import torch
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    import mytinygl_gb300 as M
+
+    M.build()
+    lib = M.library()
+    scenes = W.serve_scenes(32)
+    ctxs = []
+    srv = lib.server(executors=2, max_batch=64)
+    for sc in scenes:
+        c = lib.context(sc.width, sc.height)
+        k = W.frame_start(sc)
+        sc.play(c, 0, k)
+        c.glFinish()
+        ctxs.append(c)
+        srv.add_scene(c, sc.stream(k), W.scene_triangles(sc))
+    rate = 2000.0
+    # warm-up: capacities learned, graphs captured, framebuffer pool filled
+    for i in range(args.warmup):
+        warm = W.serve_trace(0.5, rate, seed=100 + i)
+        srv.run_trace(_serve_requests(warm, srv.now() + 0.01))
+    trace = W.serve_trace(args.serve_seconds, rate, seed=6)
+    reqs = _serve_requests(trace, srv.now() + 0.05)
+    with ClockSampler(local) as clocks:
+        st0 = srv.stats()
+        srv.run_trace(reqs)
+        st1 = srv.stats()
+    summ = _latency_summary(reqs)
+    busy = st1["busy_seconds"] - st0["busy_seconds"]
+    batches = st1["batches"] - st0["batches"]
+
+    # e2e: every frame read back into a ring of page-locked buffers per resolution
+    ring = 4 * 64 + 32  # more than executors x max_batch requests can be in flight
+    pinned = {}
+    for w, h in W.SERVE_RESOLUTIONS:
+        pinned[(w, h)] = [torch.empty(w * h, dtype=torch.int32, pin_memory=True) for _ in range(ring)]
+    count = {}
+
+    def out_for(i, w, h):
+        j = count.get((w, h), 0)
+        count[(w, h)] = j + 1
+        return pinned[(w, h)][j % ring].data_ptr()
+
+    etrace = W.serve_trace(min(10.0, args.serve_seconds), rate, seed=7)
+    ereqs = _serve_requests(etrace, srv.now() + 0.05, out_for)
+    srv.run_trace(ereqs)
+    esumm = _latency_summary(ereqs)
+    d2h = sum(w * h * 4 for _, _, w, h, _ in etrace) / max(1, len(etrace))
+    srv.destroy()
+    for c in ctxs:
+        c.destroy()
+    out = {
+        "metric": "frames/s", "value": summ["frames_per_s"], "unit": "frames/s", "n_gpus": world,
+        "steps": len(reqs), "warmup": args.warmup, "ms_per_step": summ["mean_ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; mytinygl_gb300/workloads.py serve_scenes / serve_trace)",
+        "config": {"workload": spec["name"], "description": spec["desc"], "offered_rate": rate,
+                   "duration_s": args.serve_seconds, "requests": len(reqs), "executors": 2, "max_batch": 64,
+                   "memory_budget_gib": 40, "parallelism": f"replicas x{world}"},
+        "latency_ms": {"p50": summ["p50_ms"], "p99": summ["p99_ms"], "mean": summ["mean_ms"],
+                       "max": summ["max_ms"]},
+        "served": summ, "batches": batches,
+        "gpu_busy_fraction": round(busy / max(1e-9, max(r.finished for r in reqs) - min(r.arrival for r in reqs)), 3),
+        "deferred_for_budget": st1["deferred_for_budget"] - st0["deferred_for_budget"],
+        "peak_gib_admitted": round(st1["peak_bytes_admitted"] / 2**30, 3),
+        "e2e": {"value": esumm["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(d2h), "latency_ms": {"p50": esumm["p50_ms"], "p99": esumm["p99_ms"]}},
+        "gpu_launches": None, "clocks": clocks.summary(),
+    }
+    return out if rank == 0 else None
+
+
 def cpu_batch_frames(lib, scenes, threads):
     """Render each scene once on the oracle, one context per thread; returns wall seconds."""
     def one(sc):
@@ -682,6 +790,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="textured")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline work per thread")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving trace length (workload serve)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
     spec = WORKLOADS[args.workload]
@@ -689,6 +798,8 @@ def main():
         out = run_reference(args, spec)
     elif args.workload == "batch":
         out = run_batch(args, spec)
+    elif args.workload == "serve":
+        out = run_serve(args, spec)
     else:
         out = run_ours(args, spec)
     if out is not None:

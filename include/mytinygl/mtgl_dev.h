@@ -241,8 +241,20 @@ int mtgl_dev_batch_destroy(mtgl_batch *b);
  * batch and returns without waiting; a previous submission of b is waited for first.
  * Afterwards each context reads, flushes or changes resources only after the batch. */
 int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n);
+/* The same, step by step: begin (waits for the previous submission), then any number of
+ * add (src's pending pass, recorded on src with its resources, renders into target's
+ * framebuffer; targets are distinct within a batch, a source may give several passes),
+ * readback (after the run, copy target's colour buffer to host memory; page-locked memory
+ * keeps the copy asynchronous), then launch. */
+int mtgl_dev_batch_begin(mtgl_batch *b);
+int mtgl_dev_batch_add(mtgl_batch *b, mtgl_dev *src, mtgl_dev *target);
+int mtgl_dev_batch_readback(mtgl_batch *b, mtgl_dev *target, uint32_t *host_color);
+int mtgl_dev_batch_launch(mtgl_batch *b);
 /* Waits for the last submission and checks its capacities (see above). */
 int mtgl_dev_batch_wait(mtgl_batch *b);
+/* 1 when the last submission has finished on the device (mtgl_dev_batch_wait then returns
+ * without blocking unless the run overflowed), 0 while it runs, negative on error. */
+int mtgl_dev_batch_query(mtgl_batch *b);
 int mtgl_dev_batch_stats(mtgl_batch *b, mtgl_batch_stats *out);
 int mtgl_dev_batch_reset_stats(mtgl_batch *b);
 /* The cudaStream_t the batch runs on. */

@@ -21,6 +21,7 @@ REPO = os.path.dirname(PKG)
 INCLUDE = os.path.join(REPO, "include")
 FRONT_DIR = os.path.join(PKG, "csrc", "front")
 DEV_DIR = os.path.join(PKG, "csrc", "dev")
+SERVE_DIR = os.path.join(PKG, "csrc", "serve")
 LIB_DIR = os.path.join(PKG, "lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libmytinygl_gb300.so")
@@ -73,11 +74,11 @@ def build(verbose=False, force=False) -> str:
         objs.append(obj)
         if force or _stale(obj, src, headers):
             jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
-    for src in sorted(glob.glob(os.path.join(FRONT_DIR, "*.c"))):
+    for src in sorted(glob.glob(os.path.join(FRONT_DIR, "*.c")) + glob.glob(os.path.join(SERVE_DIR, "*.c"))):
         obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, src, headers):
-            jobs.append(["gcc"] + CC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append(["gcc"] + CC_FLAGS + ["-pthread", "-c", src, "-o", obj])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             futs = [ex.submit(_run, j, j[-1] + ".log") for j in jobs]
@@ -87,7 +88,7 @@ def build(verbose=False, force=False) -> str:
         tmp = LIB_PATH + ".tmp"
         _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs +
              ["-Xlinker", "-Bsymbolic", "-Xlinker", "--exclude-libs,ALL", "-Xlinker",
-              f"--version-script={EXPORTS}", "-lm"], os.path.join(OBJ_DIR, "link.log"))
+              f"--version-script={EXPORTS}", "-lm", "-lpthread"], os.path.join(OBJ_DIR, "link.log"))
         os.replace(tmp, LIB_PATH)
     if verbose:
         print(f"built {LIB_PATH} ({len(jobs)} objects rebuilt)")

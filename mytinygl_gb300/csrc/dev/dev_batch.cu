@@ -52,11 +52,16 @@ struct mtgl_batch {
     int tile_shift = 4;
     uint32_t rec_cap = 0, pair_cap = 0;  // capacities learned from the totals seen so far
     cudaEvent_t done = nullptr;
-    // the submission in flight
+    // the submission being built (open) or in flight (pending)
+    bool open = false;
     bool pending = false;
-    std::vector<mtgl_dev *> devs;
+    std::vector<mtgl_dev *> devs;     // contexts whose framebuffer the run writes, once each
+    std::vector<mtgl_dev *> sources;  // contexts whose resources it only reads, once each
     std::vector<Pass> passes;
-    std::vector<FrameSrc> frames;
+    std::vector<FrameSrc> frames;     // frame f renders passes[f] into frames[f].dev
+    std::vector<std::pair<mtgl_dev *, uint32_t *>> readbacks;
+    uint64_t open_tris = 0;
+    bool ran = false;                 // the pending submission ran the pipeline (not readbacks only)
     Tables t;
     PipeConfig run{};
     // graph of the last capacity-mode run
@@ -72,6 +77,10 @@ namespace {
 
 int record_after(mtgl_batch *b)
 {
+    for (const auto &rb : b->readbacks) {
+        const size_t n = (size_t)rb.first->width * (size_t)rb.first->height;
+        CK(cudaMemcpyAsync(rb.second, rb.first->color, n * 4, cudaMemcpyDeviceToHost, b->x.stream));
+    }
     for (mtgl_dev *d : b->devs) {
         CK(cudaEventRecord(d->after_batch, b->x.stream));
         d->wait_batch = true;
@@ -222,54 +231,129 @@ int mtgl_dev_batch_destroy(mtgl_batch *b)
     return MTGL_OK;
 }
 
-int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
+int mtgl_dev_batch_begin(mtgl_batch *b)
 {
-    if (!b || n < 0 || (n > 0 && !devs)) return MTGL_ERR_INVALID;
+    if (!b) return MTGL_ERR_INVALID;
     CK(cudaSetDevice(b->x.device));
     int st = mtgl_dev_batch_wait(b);
-    if (st) return st;
-    for (int32_t i = 0; i < n; i++) {
-        mtgl_dev *d = devs[i];
-        if (!d || d->device != b->x.device) return MTGL_ERR_INVALID;
-        for (int32_t j = 0; j < i; j++)
-            if (devs[j] == d) return MTGL_ERR_INVALID;  // a context renders one pass per batch
-        if (d->batch && (st = mtgl_dev_batch_wait(d->batch))) return st;
-    }
-    if ((st = b->stage.wait())) return st;
+    if (st || (st = b->stage.wait())) return st;
     b->stage.used = 0;
     b->devs.clear();
+    b->sources.clear();
     b->passes.clear();
     b->frames.clear();
-    b->passes.reserve((size_t)n);
-    uint64_t tris = 0;
-    for (int32_t i = 0; i < n; i++) {
-        mtgl_dev *d = devs[i];
-        if (d->pass.empty()) continue;
-        // order the batch after work already queued on the context's stream, and after a
-        // batch of another executor the context's stream has not waited for yet
-        if (d->dirty) {
-            CK(cudaEventRecord(d->tail, d->x.stream));
-            CK(cudaStreamWaitEvent(b->x.stream, d->tail, 0));
-            d->dirty = false;
-        }
-        if (d->wait_batch) CK(cudaStreamWaitEvent(b->x.stream, d->after_batch, 0));
-        int64_t off = 0;
-        if ((st = b->stage.reserve(d->stage.used, &off))) return st;
-        if (d->stage.used) memcpy(b->stage.p + off, d->stage.p, d->stage.used);
-        b->passes.push_back(std::move(d->pass));
-        d->pass.reset();
-        d->stage.used = 0;
-        b->devs.push_back(d);
-        b->frames.push_back(FrameSrc{d, nullptr, off});
-        tris += b->passes.back().tris;
-        d->stats.passes++;
-        d->stats.input_triangles += b->passes.back().tris;
+    b->readbacks.clear();
+    b->open_tris = 0;
+    b->open = true;
+    return MTGL_OK;
+}
+
+namespace {
+
+// Puts d in the run's context sets once, ordering the batch stream after d's queued work.
+// A written context (a target framebuffer) is also ordered after any batch of another
+// executor that wrote it; a context whose resources are only read needs no order against
+// other batches that only read them, so batches sharing a scene still run side by side.
+int involve(mtgl_batch *b, mtgl_dev *d, bool write)
+{
+    if (d->device != b->x.device) return MTGL_ERR_INVALID;
+    bool known = false;
+    for (mtgl_dev *e : b->devs) known = known || e == d;
+    for (mtgl_dev *e : b->sources) known = known || e == d;
+    if (!known && d->dirty) {
+        CK(cudaEventRecord(d->tail, d->x.stream));
+        CK(cudaStreamWaitEvent(b->x.stream, d->tail, 0));
+        d->dirty = false;
     }
-    if (b->devs.empty()) return MTGL_OK;
+    if (!write) {
+        if (!known) b->sources.push_back(d);
+        return MTGL_OK;
+    }
+    for (mtgl_dev *e : b->devs)
+        if (e == d) return MTGL_OK;
+    if (d->batch && d->batch != b) {
+        int st = mtgl_dev_batch_wait(d->batch);
+        if (st) return st;
+    }
+    if (d->wait_batch) CK(cudaStreamWaitEvent(b->x.stream, d->after_batch, 0));
+    b->devs.push_back(d);
+    return MTGL_OK;
+}
+
+// marks the run's contexts: targets wait for it through their stream, sources list it as a
+// reader their next device operation waits for
+void attach(mtgl_batch *b)
+{
+    for (mtgl_dev *d : b->devs) d->batch = b;
+    for (mtgl_dev *d : b->sources) {
+        bool written = false;
+        for (mtgl_dev *e : b->devs) written = written || e == d;
+        if (!written) d->readers.push_back(b);
+    }
+}
+
+void detach(mtgl_batch *b)
+{
+    for (mtgl_dev *d : b->devs)
+        if (d->batch == b) d->batch = nullptr;
+    for (mtgl_dev *d : b->sources)
+        for (size_t i = 0; i < d->readers.size(); i++)
+            if (d->readers[i] == b) {
+                d->readers.erase(d->readers.begin() + (long)i);
+                break;
+            }
+}
+
+}  // namespace
+
+int mtgl_dev_batch_add(mtgl_batch *b, mtgl_dev *src, mtgl_dev *target)
+{
+    if (!b || !src || !target || !b->open) return MTGL_ERR_INVALID;
+    for (const FrameSrc &f : b->frames)
+        if (f.dev == target) return MTGL_ERR_INVALID;  // two frames of one batch cannot share a framebuffer
+    if (src->pass.empty()) return MTGL_OK;
+    int st;
+    if ((st = involve(b, src, src == target)) || (st = involve(b, target, true))) return st;
+    int64_t off = 0;
+    if ((st = b->stage.reserve(src->stage.used, &off))) return st;
+    if (src->stage.used) memcpy(b->stage.p + off, src->stage.p, src->stage.used);
+    b->passes.push_back(std::move(src->pass));
+    src->pass.reset();
+    src->stage.used = 0;
+    b->frames.push_back(FrameSrc{target, nullptr, off});
+    b->open_tris += b->passes.back().tris;
+    src->stats.passes++;
+    src->stats.input_triangles += b->passes.back().tris;
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_readback(mtgl_batch *b, mtgl_dev *target, uint32_t *host_color)
+{
+    if (!b || !target || !host_color || !b->open) return MTGL_ERR_INVALID;
+    int st = involve(b, target, true);
+    if (st) return st;
+    b->readbacks.emplace_back(target, host_color);
+    return MTGL_OK;
+}
+
+int mtgl_dev_batch_launch(mtgl_batch *b)
+{
+    if (!b || !b->open) return MTGL_ERR_INVALID;
+    CK(cudaSetDevice(b->x.device));
+    b->open = false;
+    int st;
+    if (b->frames.empty()) {
+        if (b->readbacks.empty()) return MTGL_OK;
+        if ((st = record_after(b))) return st;  // readbacks only
+        attach(b);
+        b->pending = true;
+        b->ran = false;
+        return MTGL_OK;
+    }
     for (size_t i = 0; i < b->frames.size(); i++) b->frames[i].pass = &b->passes[i];
     if ((st = build_tables(b->x, b->stage, b->frames.data(), (uint32_t)b->frames.size(), b->tile_shift, true, b->t)))
         return st;
-
+    const uint64_t tris = b->open_tris;
     // capacities: the larger of the learned totals and the configured factors
     const uint64_t rec_want = std::max<uint64_t>((uint64_t)b->rec_cap, (uint64_t)(tris * b->cfg.record_factor) + 1);
     const uint32_t rec_cap = tris ? round_capacity(rec_want) : 0;
@@ -284,13 +368,43 @@ int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
     if ((st = launch_run(b))) return st;
     if ((st = b->stage.mark_uploaded(b->x.stream))) return st;
     if ((st = record_after(b))) return st;
-    for (mtgl_dev *d : b->devs) d->batch = b;
+    attach(b);
     b->pending = true;
+    b->ran = true;
     b->stats.batches++;
-    b->stats.frames += b->devs.size();
+    b->stats.frames += b->frames.size();
     b->stats.input_triangles += tris;
     b->stats.ctas = b->run.ctas;
     return MTGL_OK;
+}
+
+int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
+{
+    if (!b || n < 0 || (n > 0 && !devs)) return MTGL_ERR_INVALID;
+    for (int32_t i = 0; i < n; i++) {
+        if (!devs[i]) return MTGL_ERR_INVALID;
+        for (int32_t j = 0; j < i; j++)
+            if (devs[j] == devs[i]) return MTGL_ERR_INVALID;  // a context renders one pass per batch
+    }
+    int st = mtgl_dev_batch_begin(b);
+    if (st) return st;
+    for (int32_t i = 0; i < n; i++) {
+        if ((st = mtgl_dev_batch_add(b, devs[i], devs[i]))) {
+            b->open = false;
+            return st;
+        }
+    }
+    return mtgl_dev_batch_launch(b);
+}
+
+int mtgl_dev_batch_query(mtgl_batch *b)
+{
+    if (!b) return MTGL_ERR_INVALID;
+    if (!b->pending) return 1;
+    cudaError_t e = cudaEventQuery(b->done);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return -fail_cuda("cudaEventQuery", e);
 }
 
 int mtgl_dev_batch_wait(mtgl_batch *b)
@@ -299,8 +413,14 @@ int mtgl_dev_batch_wait(mtgl_batch *b)
     if (!b->pending) return MTGL_OK;
     CK(cudaSetDevice(b->x.device));
     b->pending = false;  // a failure below leaves nothing to retry
-    for (mtgl_dev *d : b->devs) d->batch = nullptr;
+    detach(b);
     CK(cudaEventSynchronize(b->done));
+    if (!b->ran) {
+        b->devs.clear();
+        b->sources.clear();
+        b->readbacks.clear();
+        return MTGL_OK;
+    }
     uint32_t nrec = b->x.h_totals[0], npairs = b->x.h_totals[1];
     if (nrec > b->run.rec_cap || npairs > b->run.pair_cap) {
         // The tile launch left every framebuffer untouched: render again with exact sizing
@@ -325,8 +445,10 @@ int mtgl_dev_batch_wait(mtgl_batch *b)
     b->stats.record_capacity = b->run.rec_cap;
     b->stats.pair_capacity = b->run.pair_cap;
     b->devs.clear();
+    b->sources.clear();
     b->passes.clear();
     b->frames.clear();
+    b->readbacks.clear();
     return MTGL_OK;
 }
 

@@ -186,7 +186,8 @@ struct mtgl_dev {
     bool dirty = false;
     cudaEvent_t after_batch = nullptr;
     bool wait_batch = false;
-    mtgl_batch *batch = nullptr;  // an unverified batch this context's frame belongs to
+    mtgl_batch *batch = nullptr;  // an unverified batch that writes this context's framebuffer
+    std::vector<mtgl_batch *> readers;  // unfinished batches that read this context's resources
 };
 
 // Every entry that enqueues work on a context's stream goes through here first.

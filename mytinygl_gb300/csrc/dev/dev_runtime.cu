@@ -150,10 +150,24 @@ int flush_if_drawing(mtgl_dev *d)
 
 }  // namespace
 
+// For the serving loop (csrc/serve): the device a context lives on, and binding a thread to
+// it. Internal to the library (not exported).
+extern "C" int dev_device_index(const mtgl_dev *d) { return d ? d->device : -1; }
+extern "C" int dev_bind_thread(int device) { return cudaSetDevice(device) == cudaSuccess ? MTGL_OK : MTGL_ERR_CUDA; }
+extern "C" int dev_current_device(void)
+{
+    int d = 0;
+    return cudaGetDevice(&d) == cudaSuccess ? d : -1;
+}
+
 int mtgl_dev_enter(mtgl_dev *d)
 {
     if (d->batch) {
         int st = mtgl_dev_batch_wait(d->batch);  // verifies (and if needed re-runs) the batch
+        if (st) return st;
+    }
+    while (!d->readers.empty()) {  // batches still reading this context's resources
+        int st = mtgl_dev_batch_wait(d->readers.back());
         if (st) return st;
     }
     if (d->wait_batch) {

@@ -208,12 +208,29 @@ __device__ __forceinline__ void snap_plane(CV &v, int p)
 // those extra vertices are dropped instead of written out of bounds.
 constexpr int kClipMax = 12;
 
-// clip_triangle (clipping.h:106-126): six Sutherland-Hodgman passes; result in bufA[0..n)
-__device__ __noinline__ int clip_triangle(CV *bufA, CV *bufB)
+// Where clip_triangle's six passes can start. A pass over a triangle whose three vertices
+// are all inside its plane copies them unchanged, in order, so passes are skipped while that
+// holds; at the first plane with all three outside the pass returns an empty polygon, so the
+// triangle produces nothing. Returns 0..5 (the first pass that must run), kClipNone (all
+// inside: no clipping) or kClipEmpty.
+constexpr int kClipNone = 6, kClipEmpty = 7;
+__device__ __forceinline__ int clip_start(const float4 &a, const float4 &b, const float4 &c)
+{
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+        const bool ia = plane_dist(a, p) >= 0.0f, ib = plane_dist(b, p) >= 0.0f, ic = plane_dist(c, p) >= 0.0f;
+        if (!(ia && ib && ic)) return (ia || ib || ic) ? p : kClipEmpty;
+    }
+    return kClipNone;
+}
+
+// clip_triangle (clipping.h:106-126): Sutherland-Hodgman passes from plane `first` on (the
+// earlier ones copy the triangle unchanged, see clip_start); result in bufA[0..n)
+__device__ __noinline__ int clip_triangle(CV *bufA, CV *bufB, int first)
 {
     int n = 3;
     CV *in = bufA, *out = bufB;
-    for (int p = 0; p < 6; p++) {
+    for (int p = first; p < 6; p++) {
         int m = 0;
         const CV *prev = &in[n - 1];
         float pd = plane_dist(prev->clip, p);
@@ -474,6 +491,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.total_tris) return;
+    if (EMIT && A.tri_counts[t] == 0) return;  // the count pass found nothing to emit
     const int d = find_base(A.draw_tri_base, A.ndraws, t);
     const DevDraw &D = A.draws[d];
     const uint32_t k = t - D.tri_base;
@@ -489,12 +507,12 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
     load_cv(A, element_slot(D, e1), eye, v1);
     load_cv(A, element_slot(D, e2), eye, v2);
 
-    // all three vertices inside all six planes: the clipper returns the triangle unchanged
-    bool inside = true;
-#pragma unroll
-    for (int p = 0; p < 6; p++)
-        inside = inside && (plane_dist(v0.clip, p) >= 0.0f) && (plane_dist(v1.clip, p) >= 0.0f) &&
-                 (plane_dist(v2.clip, p) >= 0.0f);
+    const int start = clip_start(v0.clip, v1.clip, v2.clip);
+    if (start == kClipEmpty) {
+        if (!EMIT) A.tri_counts[t] = 0;
+        return;
+    }
+    const bool inside = start == kClipNone;  // the clipper would return the triangle unchanged
     const uint32_t out = EMIT ? A.tri_offsets[t] : 0;
     const bool write_eye = EMIT && eye && A.eye_records;
     uint32_t produced = 0;
@@ -511,7 +529,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
         bufA[0] = v0;
         bufA[1] = v1;
         bufA[2] = v2;
-        const int n = clip_triangle(bufA, bufB);
+        const int n = clip_triangle(bufA, bufB, start);
         if (n >= 3) {
             for (int j = 0; j < n; j++) persp_divide(bufA[j]);
             for (int j = 1; j + 1 < n; j++) {

@@ -114,6 +114,27 @@ class Timings(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class ServerConfig(ctypes.Structure):
+    """mtgl_server_config (include/mytinygl/mtgl_serve.h)"""
+    _fields_ = [("memory_budget", ctypes.c_uint64), ("max_batch", ctypes.c_int32), ("executors", ctypes.c_int32),
+                ("batch", BatchConfig)]
+
+
+class Request(ctypes.Structure):
+    """mtgl_request (include/mytinygl/mtgl_serve.h)"""
+    _fields_ = [("scene", ctypes.c_int32), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("modelview", ctypes.c_float * 16), ("color", ctypes.c_void_p), ("arrival", ctypes.c_double),
+                ("admitted", ctypes.c_double), ("finished", ctypes.c_double), ("status", ctypes.c_int32),
+                ("batch_size", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    """mtgl_server_stats (include/mytinygl/mtgl_serve.h)"""
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "batches",
+                                               "deferred_for_budget", "peak_bytes_admitted",
+                                               "framebuffers_allocated")] + [("busy_seconds", ctypes.c_double)]
+
+
 class GLLibrary:
     """One loaded GL implementation (a shared library exporting include/GL/gl.h)."""
 
@@ -151,6 +172,25 @@ class GLLibrary:
         self.has_batches = hasattr(L, "mtgl_dev_batch_create")  # the reference build has none
         if self.has_batches:
             self._bind_batches(L)
+        self.has_server = hasattr(L, "mtgl_server_create")  # the GB300 library only
+        if self.has_server:
+            L.mtgl_server_create.restype = ctypes.c_int
+            L.mtgl_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
+            L.mtgl_server_destroy.restype = ctypes.c_int
+            L.mtgl_server_destroy.argtypes = [ctypes.c_void_p]
+            L.mtgl_server_add_scene.restype = ctypes.c_int
+            L.mtgl_server_add_scene.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                ctypes.c_uint64]
+            L.mtgl_server_now.restype = ctypes.c_double
+            L.mtgl_server_now.argtypes = [ctypes.c_void_p]
+            L.mtgl_server_submit.restype = ctypes.c_int
+            L.mtgl_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request)]
+            L.mtgl_server_drain.restype = ctypes.c_int
+            L.mtgl_server_drain.argtypes = [ctypes.c_void_p]
+            L.mtgl_server_run_trace.restype = ctypes.c_int
+            L.mtgl_server_run_trace.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_int32]
+            L.mtgl_server_get_stats.restype = ctypes.c_int
+            L.mtgl_server_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ServerStats)]
 
     @staticmethod
     def _bind_batches(L):
@@ -193,6 +233,61 @@ class GLLibrary:
     def batch(self, **config) -> "Batch":
         """A batch executor; keyword arguments override fields of mtgl_batch_config."""
         return Batch(self, **config)
+
+    def server(self, memory_budget=0, max_batch=0, executors=0, **batch) -> "Server":
+        """A serving loop (mtgl_serve.h); batch keywords override fields of mtgl_batch_config."""
+        return Server(self, memory_budget, max_batch, executors, **batch)
+
+
+class Server:
+    """mtgl_server: resident scenes, requests admitted against a memory budget, batched."""
+
+    def __init__(self, glib: GLLibrary, memory_budget=0, max_batch=0, executors=0, **batch):
+        self.glib = glib
+        cfg = ServerConfig()
+        cfg.memory_budget, cfg.max_batch, cfg.executors = memory_budget, max_batch, executors
+        glib.lib.mtgl_dev_batch_defaults(ctypes.byref(cfg.batch))
+        for k, v in batch.items():
+            setattr(cfg.batch, k, v)
+        h = ctypes.c_void_p()
+        st = glib.lib.mtgl_server_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            raise RuntimeError(f"mtgl_server_create failed with status {st}")
+        self.handle = h.value
+        self._keep = []
+
+    def add_scene(self, ctx: "GLContext", stream: bytes, triangles: int) -> int:
+        buf = ctypes.create_string_buffer(stream, len(stream))
+        self._keep.append((ctx, buf))
+        sid = self.glib.lib.mtgl_server_add_scene(self.handle, ctx.handle, buf, len(stream), int(triangles))
+        if sid < 0:
+            raise RuntimeError(f"mtgl_server_add_scene failed with status {-sid}")
+        return sid
+
+    def now(self) -> float:
+        return self.glib.lib.mtgl_server_now(self.handle)
+
+    def run_trace(self, reqs):
+        """reqs: a ctypes array of Request; returns when all have finished."""
+        st = self.glib.lib.mtgl_server_run_trace(self.handle, reqs, len(reqs))
+        if st != 0:
+            raise RuntimeError(f"mtgl_server_run_trace failed with status {st}")
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        self.glib.lib.mtgl_server_get_stats(self.handle, ctypes.byref(s))
+        return {n: getattr(s, n) for n, _ in ServerStats._fields_}
+
+    def destroy(self):
+        if self.handle:
+            self.glib.lib.mtgl_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 class PreparedStreams:

@@ -169,7 +169,7 @@ TEXTURED_SPREAD = 0.33  # per-vertex offset U[-s, s]: ~30 % of the triangles str
 
 def textured_scene(width=1920, height=1080, ntri=100_000, seed=1, tex_size=512, use_vbo=True,
                    spread=TEXTURED_SPREAD, fog=True, lights=8, min_filter=G.GL_LINEAR_MIPMAP_LINEAR,
-                   rotate_z=0.0):
+                   rotate_z=0.0, modelview_from_caller=False):
     """Textured with clipping and fog: identity modelview/projection; triangle centres
     U[-1.5, 1.5]^3 in clip space with per-vertex offsets U[-s, s]^3; per-vertex RGBA8 colour
     U[0,255], uv U[0,4) with GL_REPEAT, normals U[-1,1]^3; a tex_size^2 RGBA8 noise texture
@@ -206,9 +206,10 @@ def textured_scene(width=1920, height=1080, ntri=100_000, seed=1, tex_size=512, 
     s.glMatrixMode(G.GL_PROJECTION)
     s.glLoadIdentity()
     s.glMatrixMode(G.GL_MODELVIEW)
-    s.glLoadIdentity()
-    if rotate_z:
-        s.glMultMatrixf(euler_matrix(0.0, 0.0, rotate_z))
+    if not modelview_from_caller:  # else the modelview loaded before the frame stays
+        s.glLoadIdentity()
+        if rotate_z:
+            s.glMultMatrixf(euler_matrix(0.0, 0.0, rotate_z))
     s.glBindTexture(G.GL_TEXTURE_2D, 1)
     s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MIN_FILTER, min_filter)
     s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MAG_FILTER, G.GL_LINEAR)
@@ -353,6 +354,44 @@ def uneven_frame(index, seed=3, min_side=64, max_side=1024, min_tri=100, max_tri
 def uneven_batch(nframes=256, seed=3, **kw):
     """The batched uneven-frames workload: `nframes` independent frames (uneven_frame)."""
     return [uneven_frame(i, seed=seed, **kw) for i in range(nframes)]
+
+
+SERVE_RESOLUTIONS = ((256, 256), (512, 512), (1280, 720), (1920, 1080))
+
+
+def serve_scenes(nscenes=32, seed=5, min_tri=1000, max_tri=500_000, tex_sizes=(256, 512, 1024, 2048),
+                 width=1920, height=1080):
+    """Resident scenes of the serving workload, built like the textured frame (clip-straddling
+    triangles, 8 point lights, EXP fog, trilinear texture): triangle counts log-uniform in
+    [min_tri, max_tri], power-of-two textures log-uniform over tex_sizes. The frame part
+    (from the first glClear) takes its modelview from the caller."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(nscenes):
+        ntri = int(round(_log_uniform(rng, min_tri, max_tri)))
+        tex = int(tex_sizes[int(rng.integers(0, len(tex_sizes)))])
+        s = textured_scene(width, height, ntri=ntri, seed=int(rng.integers(0, 2**31 - 1)), tex_size=tex,
+                           modelview_from_caller=True)
+        s.name = f"serve_scene{i}"
+        out.append(s)
+    return out
+
+
+def serve_trace(duration_s=60.0, rate=2000.0, nscenes=32, seed=6, resolutions=SERVE_RESOLUTIONS):
+    """Poisson arrivals at `rate` per second for `duration_s`: (arrival s, scene, width,
+    height, modelview) with the scene uniform, the resolution uniform over `resolutions`
+    and the modelview a rotation drawn from the request's own seed."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration_s:
+            break
+        w, h = resolutions[int(rng.integers(0, len(resolutions)))]
+        r = np.random.default_rng([seed, len(out)])
+        mv = euler_matrix(r.uniform(-0.3, 0.3), r.uniform(-0.3, 0.3), r.uniform(0.0, 2 * math.pi))
+        out.append((t, int(rng.integers(0, nscenes)), w, h, mv))
+    return out
 
 
 def scene_triangles(scene: Scene) -> int:

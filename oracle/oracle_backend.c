@@ -1440,6 +1440,23 @@ int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
 }
 
 int mtgl_dev_batch_wait(mtgl_batch *b) { return b ? MTGL_OK : MTGL_ERR_INVALID; }
+int mtgl_dev_batch_query(mtgl_batch *b) { return b ? 1 : -MTGL_ERR_INVALID; }
+int mtgl_dev_batch_begin(mtgl_batch *b) { return b ? MTGL_OK : MTGL_ERR_INVALID; }
+int mtgl_dev_batch_launch(mtgl_batch *b) { return b ? MTGL_OK : MTGL_ERR_INVALID; }
+
+/* The oracle's contexts hold their own framebuffers and render at once: a pass recorded
+ * on one context cannot be retargeted. */
+int mtgl_dev_batch_add(mtgl_batch *b, mtgl_dev *src, mtgl_dev *target)
+{
+    if (!b || !src || !target) return MTGL_ERR_INVALID;
+    return src == target ? MTGL_OK : MTGL_ERR_UNSUPPORTED;
+}
+
+int mtgl_dev_batch_readback(mtgl_batch *b, mtgl_dev *target, uint32_t *host_color)
+{
+    if (!b || !target || !host_color) return MTGL_ERR_INVALID;
+    return mtgl_dev_read(target, host_color, NULL, NULL);
+}
 
 int mtgl_dev_batch_stats(mtgl_batch *b, mtgl_batch_stats *out)
 {

@@ -1,24 +1,28 @@
 #!/usr/bin/env python3
 """Headline benchmark: frames/s of the fixed-function pipeline on one GB300.
 
-Workload (default): the textured configuration — 1920x1080, 100k triangles whose clip-space
-vertices spill 1.5x past the frustum (~30 % clipped), per-vertex RGBA8 colour, uv in [0,4)
-with GL_REPEAT, a 512x512 RGBA8 noise texture sampled GL_LINEAR_MIPMAP_LINEAR and
-GL_MODULATE, 8 point lights with GL_COLOR_MATERIAL, GL_EXP fog (density 0.5), depth test
-GL_LESS. Seeded synthetic inputs (mytinygl_gb300/workloads.py), no dataset.
+Workload (default `batch`): 256 independent frames per step — sides log-uniform 64-1024,
+triangle counts log-uniform 100-200k, each a lit UV sphere or a textured frame with ~30 %
+clipped triangles (p = 1/2), with its own modelview, lights and 256x256 mipmapped texture —
+rendered by one batched pipeline run (mtgl_batch_render: persistent tile kernel over all
+frames, CUDA graph replay), and compared with the plain per-frame path on the same frames.
+Other workloads: `textured` (1920x1080, 100k clip-straddling triangles, 512^2 trilinear
+texture, 8 point lights, EXP fog), `rop` (1920x1080, 1M small blended triangles with
+alpha, stencil and depth tests), `sphere` (800x600 lit UV sphere), `serve` (Poisson
+requests at 2,000/s against 32 resident scenes through the C serving loop). Seeded
+synthetic inputs (mytinygl_gb300/workloads.py), no dataset.
 
-A step is one frame: glClear, the frame's state calls and the glDrawArrays, submitted with
-glFlush. Lines printed (one JSON object each, rank 0 only):
-  value        frames/s with the vertex buffer and texture resident in device memory, timed
-               with CUDA events on the renderer's own stream; L2 is flushed (a 256 MiB write
-               on that stream) before every timed frame.
-  e2e          frames/s through the public C ABI with client vertex arrays: every step
-               copies the frame's vertex arrays host->device and reads the colour buffer
-               back (mtgl_read_framebuffer), timed on the host clock.
+Lines printed (one JSON object each, rank 0 only):
+  value        frames/s with inputs resident in device memory, timed with CUDA events on
+               the stream the work runs on (the batch's, or the context's for single
+               frames); L2 is flushed (a 256 MiB write on that stream) before every step.
+  e2e          the same frames through the public C ABI with host inputs (client vertex
+               arrays copied host->device every step) and every colour buffer read back,
+               timed on the host clock.
   roofline     the tile raster/ROP kernel (K4): compulsory bytes per launch over its mean
-               launch time (CUDA events around the launch), against the measured HBM copy peak.
+               launch time (CUDA events inside the library), against the measured HBM copy peak.
   cpu_baseline the CPU oracle (a restatement of MyTinyGL's renderer) on all host cores, one
-               context per thread, on a bounded sample of the same frame.
+               context per thread, on a bounded sample of the same workload.
 --impl reference times that CPU implementation as the measured arm.
 Several GPUs run independent replicas (one process per GPU, no collective on the data path).
 """
@@ -62,7 +66,7 @@ WORKLOADS["serve"] = dict(builder=None, full_tris=None, name="serve_32_scenes_po
                                 "uniform over 256^2, 512^2, 1280x720, 1920x1080, modelview from the request "
                                 "seed, 40 GiB framebuffer + pipeline-scratch budget"))
 REC_BYTES = 224  # triangle record written by the setup kernel, read by the tile kernel
-BATCH_FRAMES = 256
+BATCH_FRAMES = 256  # frames per step of the batch workload (--frames changes it for profiling)
 
 
 class Stats(ctypes.Structure):
@@ -787,12 +791,15 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="textured")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batch")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline work per thread")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving trace length (workload serve)")
+    ap.add_argument("--frames", type=int, default=256, help="frames per step of the batch workload")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps
+    global BATCH_FRAMES
+    BATCH_FRAMES = args.frames
     spec = WORKLOADS[args.workload]
     if args.impl == "reference":
         out = run_reference(args, spec)

@@ -655,7 +655,50 @@ def run_serve(args, spec):
                 "d2h_bytes_per_step": int(d2h), "latency_ms": {"p50": esumm["p50_ms"], "p99": esumm["p99_ms"]}},
         "gpu_launches": None, "clocks": clocks.summary(),
     }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        times = cpu_serve_sample(_oracle_lib(), args.cpu_seconds, threads)
+        out["cpu_baseline"] = {"value": round(threads / statistics.mean(times), 4), "unit": "frames/s",
+                               "cores": threads, "kind": "port",
+                               "sample": (f"{len(times)} requests of the trace, each frame on its own oracle "
+                                          f"context, {threads} threads; frames/s = threads / mean frame time")}
     return out if rank == 0 else None
+
+
+def cpu_serve_sample(lib, seconds, threads):
+    """Oracle frames of serving requests, concurrently on `threads` cores: each request's scene
+    is set up on a context of the request's size (untimed), then its frame is timed. Takes
+    requests of the trace in order until about `seconds` of work per thread is done."""
+    scenes = W.serve_scenes(32)
+    trace = W.serve_trace(60.0, 2000.0, seed=6)
+    lock = threading.Lock()
+    state = {"next": 0, "times": [], "spent": 0.0}
+
+    def work(_):
+        while True:
+            with lock:
+                if state["spent"] >= seconds * threads or state["next"] >= len(trace):
+                    return
+                i = state["next"]
+                state["next"] += 1
+            _, sc, w, h, mv = trace[i]
+            scene = scenes[sc]
+            k = W.frame_start(scene)
+            c = lib.context(w, h)
+            scene.play(c, 0, k)
+            c.glViewport(0, 0, w, h)
+            c.glMatrixMode(G.GL_MODELVIEW)
+            c.glLoadMatrixf(np.asarray(mv, np.float32))
+            t0 = time.perf_counter()
+            scene.play(c, k)
+            dt = time.perf_counter() - t0
+            c.destroy()
+            with lock:
+                state["times"].append(dt)
+                state["spent"] += dt
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(work, range(threads)))
+    return state["times"]
 
 
 def cpu_batch_frames(lib, scenes, threads):
@@ -738,6 +781,26 @@ def run_reference(args, spec):
     if rank != 0:
         return None
     lib = _oracle_lib()
+    if spec is WORKLOADS["serve"]:
+        threads = os.cpu_count() or 1
+        budget = 120.0 / max(1, args.steps + args.warmup)
+        cpu_serve_sample(lib, min(2.0, budget), threads)  # warm-up
+        times = cpu_serve_sample(lib, budget * (args.steps / max(1, args.steps)), threads)
+        fps = threads / statistics.mean(times)
+        desc = (f"{len(times)} requests of the trace in order, each frame rendered on its own oracle context "
+                f"(scene set-up untimed), {threads} threads at once; frames/s = threads / mean frame time")
+        return {"impl": "reference", "metric": "frames/s", "value": round(fps, 4), "unit": "frames/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(statistics.mean(times) * 1e3, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded; mytinygl_gb300/workloads.py serve_scenes / serve_trace)",
+                "config": {"workload": spec["name"], "description": spec["desc"]},
+                "latency_ms": {"p50": round(float(np.percentile(times, 50)) * 1e3, 3),
+                               "p99": round(float(np.percentile(times, 99)) * 1e3, 3)},
+                "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                                 "sample": desc},
+                "e2e": {"value": round(fps, 4), "unit": "frames/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
     if spec is WORKLOADS["batch"]:
         sample, k, threads = cpu_batch_sample(120.0 / max(1, args.steps + args.warmup))
         for _ in range(args.warmup):

@@ -20,9 +20,14 @@ using namespace mtgl;
 
 namespace {
 
+// primitives of a draw: what K2 runs one thread for (points, line segments or triangles)
 uint64_t triangles_of(uint32_t mode, int64_t n)
 {
     switch (mode) {
+    case GL_POINTS: return (uint64_t)(n > 0 ? n : 0);
+    case GL_LINES: return (uint64_t)(n / 2);
+    case GL_LINE_STRIP: return n >= 2 ? (uint64_t)(n - 1) : 0;
+    case GL_LINE_LOOP: return n >= 2 ? (uint64_t)n : 0;
     case GL_TRIANGLES: return (uint64_t)(n / 3);
     case GL_TRIANGLE_STRIP:
     case GL_TRIANGLE_FAN:
@@ -371,14 +376,6 @@ int mtgl_dev_draw(mtgl_dev *d, const mtgl_draw *dr)
     CK(cudaSetDevice(d->device));
     const mtgl_raster_state *rs = dr->raster_state;
     if (dr->mode > GL_POLYGON) return MTGL_ERR_INVALID;
-    if (dr->mode < GL_TRIANGLES) {
-        snprintf(g_err, sizeof(g_err), "points and lines are not rendered by this back end");
-        return MTGL_ERR_UNSUPPORTED;
-    }
-    if (rs->polygon_mode_front != GL_FILL || rs->polygon_mode_back != GL_FILL) {
-        snprintf(g_err, sizeof(g_err), "glPolygonMode GL_POINT/GL_LINE is not rendered by this back end");
-        return MTGL_ERR_UNSUPPORTED;
-    }
     d->stats.draws++;
     const uint64_t ntri = triangles_of(dr->mode, dr->count);
     if (ntri == 0) return MTGL_OK;

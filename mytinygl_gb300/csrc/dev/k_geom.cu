@@ -392,11 +392,247 @@ __device__ __forceinline__ float depth_lower_bound(const DevRaster &R, float z0,
     return fminf(dlo, dhi);
 }
 
+// ------------------------------------------------------------------ points and lines
+
+// Depth writes with a function that can raise stored depths (the tile kernel's depth
+// rejection must not trust a bound taken before such a record).
+__device__ __forceinline__ bool raises_depth(const mtgl_raster_state &rs)
+{
+    return rs.depth_test && rs.depth_mask &&
+           (rs.depth_func == GL_GREATER || rs.depth_func == GL_GEQUAL || rs.depth_func == GL_NOTEQUAL ||
+            rs.depth_func == GL_ALWAYS);
+}
+
+// Clamps [x0,x1]x[y0,y1] to the framebuffer and, when enabled, the scissor box: the pixels
+// write_line_pixel / draw_points would touch (raster.c per-pixel bounds and scissor checks).
+__device__ __forceinline__ bool clamp_box(const mtgl_raster_state &rs, const FrameDims &dims, int64_t &x0, int64_t &y0,
+                                          int64_t &x1, int64_t &y1)
+{
+    x0 = x0 < 0 ? 0 : x0;
+    y0 = y0 < 0 ? 0 : y0;
+    x1 = x1 > dims.width - 1 ? dims.width - 1 : x1;
+    y1 = y1 > dims.height - 1 ? dims.height - 1 : y1;
+    if (rs.scissor_test) {
+        const int64_t sx0 = rs.scissor[0], sy0 = rs.scissor[1];
+        const int64_t sx1 = sx0 + rs.scissor[2] - 1, sy1 = sy0 + rs.scissor[3] - 1;
+        x0 = x0 < sx0 ? sx0 : x0;
+        y0 = y0 < sy0 ? sy0 : y0;
+        x1 = x1 > sx1 ? sx1 : x1;
+        y1 = y1 > sy1 ? sy1 : y1;
+    }
+    return x0 <= x1 && y0 <= y1;
+}
+
+__device__ __forceinline__ void rec_header(float4 *r4, int64_t x0, int64_t y0, int64_t x1, int64_t y1,
+                                           uint32_t raster_id, uint32_t frame, uint32_t flags)
+{
+    r4[1].z = __int_as_float((int32_t)x0);
+    r4[1].w = __int_as_float((int32_t)y0);
+    r4[2].x = __int_as_float((int32_t)x1);
+    r4[2].y = __int_as_float((int32_t)y1);
+    r4[11].w = __uint_as_float(raster_id);
+    r4[12] = make_float4(__uint_as_float(flags), 0.0f, 0.0f, 0.0f);
+    r4[13].w = __uint_as_float(frame);
+    r4[3].w = 0.0f;  // no depth-rejection bound
+}
+
+// One point square of final colour c and depth `depth` (the caller applied texture, alpha
+// test and fog). Returns the records produced (0 or 1).
+__device__ __forceinline__ uint32_t point_rec(const mtgl_raster_state &rs, uint32_t raster_id, uint32_t frame,
+                                              const FrameDims &dims, int64_t x0, int64_t y0, int64_t x1, int64_t y1,
+                                              float depth, float4 c, float *rec)
+{
+    if (!clamp_box(rs, dims, x0, y0, x1, y1)) return 0;
+    if (rec) {
+        float4 *r4 = reinterpret_cast<float4 *>(rec);
+        rec_header(r4, x0, y0, x1, y1, raster_id, frame,
+                   ((uint32_t)REC_POINT << kRecTypeShift) | (raises_depth(rs) ? kFlagRaisesDepth : 0u));
+        rec[R_Z0] = depth;
+        r4[5] = c;
+    }
+    return 1;
+}
+
+// draw_point_at_screen (raster.c:777-844): a polygon-mode vertex, one pixel, vertex colour,
+// alpha test on the colour, fog from -eye_z.
+__device__ __forceinline__ uint32_t screen_point(const DevRaster &R, uint32_t raster_id, uint32_t frame,
+                                                 const FrameDims &dims, int32_t x, int32_t y, float z, float4 c,
+                                                 float ez, float *rec)
+{
+    const mtgl_raster_state &rs = R.rs;
+    if (x < 0 || x >= dims.width || y < 0 || y >= dims.height) return 0;
+    const float depth = map_depth(R, z);
+    if (rs.alpha_test && !cmp_pass(rs.alpha_func, c.w, rs.alpha_ref)) return 0;
+    if (rs.fog) c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, -ez));
+    return point_rec(rs, raster_id, frame, dims, x, y, x, y, depth, c, rec);
+}
+
+// flush_points' per-vertex part (raster.c:1020-1164): clip-volume test, divide, screen
+// position, texture at lod 0 with the alpha test on its alpha (else on the colour), fog,
+// and the point_size square.
+__device__ __forceinline__ uint32_t vertex_point(const DevRaster &R, uint32_t raster_id, uint32_t frame,
+                                                 const FrameDims &dims, const CV &v, float *rec)
+{
+    const mtgl_raster_state &rs = R.rs;
+    const float4 p = v.clip;
+    if (p.x < -p.w || p.x > p.w || p.y < -p.w || p.y > p.w || p.z < -p.w || p.z > p.w || p.w <= 0.0f) return 0;
+    const float nx = p.x / p.w, ny = p.y / p.w, nz = p.z / p.w;
+    int32_t cx, cy;
+    ndc_to_screen(rs, nx, ny, cx, cy);
+    const float depth = map_depth(R, nz);
+    float4 c = v.col;
+    if (R.tex) {
+        const float4 tc = unpack_rgba(sample_lod(R, v.uv.x, v.uv.y, 0.0f));
+        if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) return 0;
+        c = make_float4(c.x * tc.x, c.y * tc.y, c.z * tc.z, c.w * tc.w);
+    } else if (rs.alpha_test && !cmp_pass(rs.alpha_func, c.w, rs.alpha_ref)) {
+        return 0;
+    }
+    if (rs.fog) c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, -v.ez));
+    int32_t ps = x86_f2i(rs.point_size + 0.5f);
+    if (ps < 1) ps = 1;
+    const int64_t xs = (int64_t)cx - ps / 2, ys = (int64_t)cy - ps / 2;
+    return point_rec(rs, raster_id, frame, dims, xs, ys, xs + ps - 1, ys + ps - 1, depth, c, rec);
+}
+
+// draw_line_full's setup (raster.c:107-241): endpoints, width and the interpolants; the tile
+// kernel finds each pixel's Bresenham step in closed form.
+__device__ __forceinline__ uint32_t line_rec(const DevRaster &R, uint32_t raster_id, uint32_t frame,
+                                             const FrameDims &dims, int32_t x0, int32_t y0, float z0, int32_t x1,
+                                             int32_t y1, float z1, float4 c0, float4 c1, float ez0, float ez1,
+                                             float2 uv0, float2 uv1, float *rec)
+{
+    const mtgl_raster_state &rs = R.rs;
+    int32_t lw = x86_f2i(rs.line_width + 0.5f);
+    if (lw < 1) lw = 1;
+    const int32_t half = lw / 2;
+    const int64_t adx = llabs((int64_t)x1 - x0), ady = llabs((int64_t)y1 - y0);
+    int64_t bx0 = x0 < x1 ? x0 : x1, bx1 = x0 < x1 ? x1 : x0;
+    int64_t by0 = y0 < y1 ? y0 : y1, by1 = y0 < y1 ? y1 : y0;
+    if (adx > ady) {  // x-major: each step writes a vertical run of lw pixels
+        by0 -= half;
+        by1 += lw - half - 1;
+    } else {          // y-major (and a single point): horizontal runs
+        bx0 -= half;
+        bx1 += lw - half - 1;
+    }
+    if (!clamp_box(rs, dims, bx0, by0, bx1, by1)) return 0;
+    if (rec) {
+        float4 *r4 = reinterpret_cast<float4 *>(rec);
+        rec_header(r4, bx0, by0, bx1, by1, raster_id, frame,
+                   ((uint32_t)REC_LINE << kRecTypeShift) | (raises_depth(rs) ? kFlagRaisesDepth : 0u));
+        r4[0] = make_float4(__int_as_float(x0), __int_as_float(y0), __int_as_float(x1), __int_as_float(y1));
+        r4[1].x = __int_as_float(lw);
+        rec[R_Z0] = z0;
+        rec[R_Z1] = z1;
+        r4[5] = c0;
+        r4[6] = c1;
+        r4[8] = make_float4(uv0.x, uv0.y, uv1.x, uv1.y);
+        rec[R_EZ0] = ez0;
+        rec[R_EZ1] = ez1;
+    }
+    return 1;
+}
+
+// clip_line (clipping.h:138-229): Cohen-Sutherland against the six planes, outside
+// endpoint first, snapping the new endpoint onto the plane. The reference's loop has no
+// bound; 32 rounds are far more than finite inputs take (each round moves one endpoint
+// onto a plane it was outside of).
+__device__ __forceinline__ int outcode(const float4 &v)
+{
+    int c = 0;
+    if (v.x < -v.w) c |= 1;
+    else if (v.x > v.w) c |= 2;
+    if (v.y < -v.w) c |= 4;
+    else if (v.y > v.w) c |= 8;
+    if (v.z < -v.w) c |= 16;
+    else if (v.z > v.w) c |= 32;
+    return c;
+}
+
+__device__ bool clip_line(CV &a, CV &b)
+{
+    int ca = outcode(a.clip), cb = outcode(b.clip);
+    for (int round = 0; round < 32; round++) {
+        if (!(ca | cb)) return true;
+        if (ca & cb) return false;
+        const int co = ca ? ca : cb;
+        const float4 &p0 = a.clip, &p1 = b.clip;
+        float d0, d1;
+        int plane;
+        if (co & 1) { d0 = p0.x + p0.w; d1 = p1.x + p1.w; plane = 2; }
+        else if (co & 2) { d0 = p0.w - p0.x; d1 = p1.w - p1.x; plane = 3; }
+        else if (co & 4) { d0 = p0.y + p0.w; d1 = p1.y + p1.w; plane = 4; }
+        else if (co & 8) { d0 = p0.w - p0.y; d1 = p1.w - p1.y; plane = 5; }
+        else if (co & 16) { d0 = p0.z + p0.w; d1 = p1.z + p1.w; plane = 0; }
+        else { d0 = p0.w - p0.z; d1 = p1.w - p1.z; plane = 1; }
+        const float denom = d0 - d1;
+        if (fabsf(denom) < 1e-10f) return false;
+        CV cl = cv_lerp(a, b, d0 / denom);
+        snap_plane(cl, plane);
+        if (co == ca) {
+            a = cl;
+            ca = outcode(a.clip);
+        } else {
+            b = cl;
+            cb = outcode(b.clip);
+        }
+    }
+    return false;
+}
+
+// draw_line_segment (raster.c:244-285): clip, divide (|w| < 1e-6 maps to the origin), screen.
+__device__ uint32_t segment_line(const DevRaster &R, uint32_t raster_id, uint32_t frame, const FrameDims &dims, CV a,
+                                 CV b, float *rec)
+{
+    if (!clip_line(a, b)) return 0;
+    float z0, z1;
+    if (fabsf(a.clip.w) >= 1e-6f) {
+        const float iw = 1.0f / a.clip.w;
+        a.clip.x *= iw;
+        a.clip.y *= iw;
+        z0 = a.clip.z * iw;
+    } else {
+        a.clip.x = 0.0f;
+        a.clip.y = 0.0f;
+        z0 = 0.0f;
+    }
+    if (fabsf(b.clip.w) >= 1e-6f) {
+        const float iw = 1.0f / b.clip.w;
+        b.clip.x *= iw;
+        b.clip.y *= iw;
+        z1 = b.clip.z * iw;
+    } else {
+        b.clip.x = 0.0f;
+        b.clip.y = 0.0f;
+        z1 = 0.0f;
+    }
+    int32_t x0, y0, x1, y1;
+    ndc_to_screen(R.rs, a.clip.x, a.clip.y, x0, y0);
+    ndc_to_screen(R.rs, b.clip.x, b.clip.y, x1, y1);
+    return line_rec(R, raster_id, frame, dims, x0, y0, z0, x1, y1, z1, a.col, b.col, a.ez, b.ez, a.uv, b.uv, rec);
+}
+
+// Where a fan triangle's records go: slot i of the primitive's output range, or nowhere
+// (count pass, or past the record capacity).
+struct RecOut {
+    float *recs, *eyes;
+    uint32_t base, cap;
+    __device__ float *rec(uint32_t i) const
+    {
+        return (recs && base + i < cap) ? recs + (size_t)(base + i) * kRecWords : nullptr;
+    }
+    __device__ float *eye(uint32_t i) const
+    {
+        return (eyes && base + i < cap) ? eyes + (size_t)(base + i) * kEyeWords : nullptr;
+    }
+};
+
 // Per fan triangle: the setup half of rasterize_triangle_smooth. Returns true when the
 // triangle produces a record; writes it when `rec` is non-null.
-__device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raster_id, uint32_t frame,
-                                              const FrameDims &dims, const CV &a, const CV &b, const CV &c, float *rec,
-                                              float *eyerec)
+__device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t raster_id, uint32_t frame,
+                                                  const FrameDims &dims, const CV &a, const CV &b, const CV &c,
+                                                  const RecOut &o, uint32_t at)
 {
     const mtgl_raster_state &rs = R.rs;
     int32_t x0, y0, x1, y1, x2, y2;
@@ -404,8 +640,35 @@ __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raste
     ndc_to_screen(rs, b.clip.x, b.clip.y, x1, y1);
     ndc_to_screen(rs, c.clip.x, c.clip.y, x2, y2);
     const float sa = idiff(x1, x0) * idiff(y2, y0) - idiff(x2, x0) * idiff(y1, y0);
-    if (culled(rs, sa)) return false;
+    if (culled(rs, sa)) return 0;
     const bool back = (rs.front_face == GL_CCW) ? (sa >= 0) : (sa < 0);
+    const uint32_t pm = back ? rs.polygon_mode_back : rs.polygon_mode_front;
+    if (pm == GL_POINT || pm == GL_LINE) {
+        // render_triangle's polygon modes (raster.c:901-958): vertex colours, lit per vertex
+        // under GL_PHONG (phong_vertex_colors), then three points or three edges
+        float4 c0 = a.col, c1 = b.col, c2 = c.col;
+        if (rs.lighting && rs.shade_model == GL_PHONG) {
+            c0 = compute_lighting(rs.lit, a.ep, a.en, rs.lit.front);
+            c1 = compute_lighting(rs.lit, b.ep, b.en, rs.lit.front);
+            c2 = compute_lighting(rs.lit, c.ep, c.en, rs.lit.front);
+        }
+        uint32_t n = 0;
+        if (pm == GL_POINT) {
+            n += screen_point(R, raster_id, frame, dims, x0, y0, a.clip.z, c0, a.ez, o.rec(at + n));
+            n += screen_point(R, raster_id, frame, dims, x1, y1, b.clip.z, c1, b.ez, o.rec(at + n));
+            n += screen_point(R, raster_id, frame, dims, x2, y2, c.clip.z, c2, c.ez, o.rec(at + n));
+        } else {
+            n += line_rec(R, raster_id, frame, dims, x0, y0, a.clip.z, x1, y1, b.clip.z, c0, c1, a.ez, b.ez, a.uv, b.uv,
+                          o.rec(at + n));
+            n += line_rec(R, raster_id, frame, dims, x1, y1, b.clip.z, x2, y2, c.clip.z, c1, c2, b.ez, c.ez, b.uv, c.uv,
+                          o.rec(at + n));
+            n += line_rec(R, raster_id, frame, dims, x2, y2, c.clip.z, x0, y0, a.clip.z, c2, c0, c.ez, a.ez, c.uv, a.uv,
+                          o.rec(at + n));
+        }
+        return n;
+    }
+    float *rec = o.rec(at);
+    float *eyerec = o.eye(at);
 
     int32_t minX = x0 < x1 ? (x0 < x2 ? x0 : x2) : (x1 < x2 ? x1 : x2);
     int32_t minY = y0 < y1 ? (y0 < y2 ? y0 : y2) : (y1 < y2 ? y1 : y2);
@@ -421,18 +684,18 @@ __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raste
         if (maxX >= rs.scissor[0] + rs.scissor[2]) maxX = rs.scissor[0] + rs.scissor[2] - 1;
         if (maxY >= rs.scissor[1] + rs.scissor[3]) maxY = rs.scissor[1] + rs.scissor[3] - 1;
     }
-    if (minX > maxX || minY > maxY) return false;
+    if (minX > maxX || minY > maxY) return 0;
     // pixels outside the framebuffer read defaults and write nothing (framebuffer.h:92-134)
     if (minX < 0) minX = 0;
     if (minY < 0) minY = 0;
     if (maxX > dims.width - 1) maxX = dims.width - 1;
     if (maxY > dims.height - 1) maxY = dims.height - 1;
-    if (minX > maxX || minY > maxY) return false;
+    if (minX > maxX || minY > maxY) return 0;
 
     const float fx0 = (float)x0, fy0 = (float)y0, fx1 = (float)x1, fy1 = (float)y1, fx2 = (float)x2, fy2 = (float)y2;
     const float area = (fx2 - fx0) * (fy1 - fy0) - (fy2 - fy0) * (fx1 - fx0);
-    if (fabsf(area) < 0.5f) return false;
-    if (!rec) return true;
+    if (fabsf(area) < 0.5f) return 0;
+    if (!rec) return 1;
 
     const float inv_area = 1.0f / area;
     float lod = 0.0f;
@@ -468,11 +731,7 @@ __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raste
     r4[11] = make_float4(a.ez, b.ez, c.ez, __uint_as_float(raster_id));
     // edge_function(a, b, p) = (px - ax) * (by - ay) - (py - ay) * (bx - ax): the per-edge
     // differences are the same floats whether formed per pixel or once here
-    const mtgl_raster_state &ds = R.rs;
-    const bool raises = ds.depth_test && ds.depth_mask &&
-                        (ds.depth_func == GL_GREATER || ds.depth_func == GL_GEQUAL || ds.depth_func == GL_NOTEQUAL ||
-                         ds.depth_func == GL_ALWAYS);
-    const uint32_t flags = (back ? 1u : 0u) | (zc << 1) | (raises ? kFlagRaisesDepth : 0u);
+    const uint32_t flags = (back ? 1u : 0u) | (zc << 1) | (raises_depth(rs) ? kFlagRaisesDepth : 0u);
     r4[12] = make_float4(__uint_as_float(flags), fy2 - fy1, fx2 - fx1, fy0 - fy2);
     r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, __uint_as_float(frame));
     if (eyerec) {
@@ -483,9 +742,24 @@ __device__ __forceinline__ bool setup_fan_tri(const DevRaster &R, uint32_t raste
         e4[3] = make_float4(c.ep.x, c.ep.y, c.ep.z, c.en.x);
         e4[4] = make_float4(c.en.y, c.en.z, 0.0f, 0.0f);
     }
-    return true;
+    return 1;
 }
 
+// vertex elements of line k of a GL_LINES / _STRIP / _LOOP draw (raster.c:1166-1196)
+__device__ __forceinline__ void element_pair(uint32_t mode, uint32_t k, uint32_t count, uint32_t &a, uint32_t &b)
+{
+    if (mode == GL_LINES) {
+        a = 2 * k;
+        b = 2 * k + 1;
+    } else {
+        a = k;
+        b = (mode == GL_LINE_LOOP && k + 1 == count) ? 0 : k + 1;
+    }
+}
+
+// K2, one thread per primitive (a point, a line or a triangle of the draw's mode). The count
+// pass stores how many records the primitive produces; the emit pass writes them at the
+// primitive's offset (exclusive scan of the counts), so records keep submission order.
 template <bool EMIT>
 __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
 {
@@ -495,49 +769,51 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
     const int d = find_base(A.draw_tri_base, A.ndraws, t);
     const DevDraw &D = A.draws[d];
     const uint32_t k = t - D.tri_base;
-    uint32_t e0, e1, e2;
-    element_triple(D.mode, k, e0, e1, e2);
     const DevRaster &R = A.rasters[D.raster];
     const bool eye = R.needs_eye && A.eyes;
     const uint32_t frame = min(R.frame, A.nframes - 1);
     const FrameDims dims = A.frames[frame].dims;
-
-    CV v0, v1, v2;
-    load_cv(A, element_slot(D, e0), eye, v0);
-    load_cv(A, element_slot(D, e1), eye, v1);
-    load_cv(A, element_slot(D, e2), eye, v2);
-
-    const int start = clip_start(v0.clip, v1.clip, v2.clip);
-    if (start == kClipEmpty) {
-        if (!EMIT) A.tri_counts[t] = 0;
-        return;
-    }
-    const bool inside = start == kClipNone;  // the clipper would return the triangle unchanged
-    const uint32_t out = EMIT ? A.tri_offsets[t] : 0;
-    const bool write_eye = EMIT && eye && A.eye_records;
+    RecOut o;
+    o.recs = EMIT ? A.records : nullptr;
+    o.eyes = (EMIT && eye) ? A.eye_records : nullptr;
+    o.base = EMIT ? A.tri_offsets[t] : 0;
+    o.cap = A.records_cap;
     uint32_t produced = 0;
-    if (inside) {
-        persp_divide(v0);
-        persp_divide(v1);
-        persp_divide(v2);
-        const bool room = out < A.records_cap;
-        float *rec = (EMIT && room) ? A.records + (size_t)out * kRecWords : nullptr;
-        float *erec = (write_eye && room) ? A.eye_records + (size_t)out * kEyeWords : nullptr;
-        if ((EMIT && !room) || setup_fan_tri(R, D.raster, frame, dims, v0, v1, v2, rec, erec)) produced = 1;
+
+    if (D.mode == GL_POINTS) {
+        CV v;
+        load_cv(A, element_slot(D, k), eye, v);
+        produced = vertex_point(R, D.raster, frame, dims, v, o.rec(0));
+    } else if (D.mode == GL_LINES || D.mode == GL_LINE_STRIP || D.mode == GL_LINE_LOOP) {
+        uint32_t e0, e1;
+        element_pair(D.mode, k, (uint32_t)D.count, e0, e1);
+        CV v0, v1;
+        load_cv(A, element_slot(D, e0), eye, v0);
+        load_cv(A, element_slot(D, e1), eye, v1);
+        produced = segment_line(R, D.raster, frame, dims, v0, v1, o.rec(0));
     } else {
-        CV bufA[kClipMax], bufB[kClipMax];
-        bufA[0] = v0;
-        bufA[1] = v1;
-        bufA[2] = v2;
-        const int n = clip_triangle(bufA, bufB, start);
-        if (n >= 3) {
-            for (int j = 0; j < n; j++) persp_divide(bufA[j]);
-            for (int j = 1; j + 1 < n; j++) {
-                const bool room = out + produced < A.records_cap;
-                if (EMIT && !room) break;
-                float *rec = EMIT ? A.records + (size_t)(out + produced) * kRecWords : nullptr;
-                float *erec = write_eye ? A.eye_records + (size_t)(out + produced) * kEyeWords : nullptr;
-                if (setup_fan_tri(R, D.raster, frame, dims, bufA[0], bufA[j], bufA[j + 1], rec, erec)) produced++;
+        uint32_t e0, e1, e2;
+        element_triple(D.mode, k, e0, e1, e2);
+        CV v0, v1, v2;
+        load_cv(A, element_slot(D, e0), eye, v0);
+        load_cv(A, element_slot(D, e1), eye, v1);
+        load_cv(A, element_slot(D, e2), eye, v2);
+        const int start = clip_start(v0.clip, v1.clip, v2.clip);
+        if (start == kClipNone) {  // the clipper would return the triangle unchanged
+            persp_divide(v0);
+            persp_divide(v1);
+            persp_divide(v2);
+            produced = setup_fan_tri(R, D.raster, frame, dims, v0, v1, v2, o, 0);
+        } else if (start != kClipEmpty) {
+            CV bufA[kClipMax], bufB[kClipMax];
+            bufA[0] = v0;
+            bufA[1] = v1;
+            bufA[2] = v2;
+            const int n = clip_triangle(bufA, bufB, start);
+            if (n >= 3) {
+                for (int j = 0; j < n; j++) persp_divide(bufA[j]);
+                for (int j = 1; j + 1 < n; j++)
+                    produced += setup_fan_tri(R, D.raster, frame, dims, bufA[0], bufA[j], bufA[j + 1], o, produced);
             }
         }
     }

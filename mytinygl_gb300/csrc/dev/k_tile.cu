@@ -151,6 +151,90 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, c
     return wrote;
 }
 
+// The pixel state a point or line fragment updates (no stencil: the reference's point and
+// line paths never touch it).
+struct PixelOut {
+    uint32_t col;
+    float dep;
+    uint32_t flags;  // bit 0: covered (a fragment); bit 1: depth written
+};
+
+// write_line_pixel (raster.c:86-104) and the pixel loop of draw_points (raster.c:1140-1160):
+// depth test, blend with the stored colour, depth write, masked colour write.
+__device__ __forceinline__ PixelOut point_ops(const mtgl_raster_state &rs, float depth, float4 c, uint32_t col,
+                                              float dep)
+{
+    PixelOut o{col, dep, 1u};
+    if (rs.depth_test && !cmp_pass(rs.depth_func, depth, dep)) return o;
+    if (rs.blend) c = blend(rs, c, unpack_rgba(col));
+    if (rs.depth_test && rs.depth_mask) {
+        o.dep = depth;
+        o.flags |= 2u;
+    }
+    o.col = masked_write(rs, col, c);
+    return o;
+}
+
+// One pixel of a point or line record (the record's bbox already holds the framebuffer and
+// scissor limits). Lines: the Bresenham step reaching this pixel in closed form. For an
+// x-major line (|dx| > |dy|) step k sits at x0 + sx*k, y0 + sy*floor((2|dy|k + |dx| - 1) /
+// (2|dx|)); for a y-major one the roles swap; each step writes a run of `lw` pixels across
+// the major axis. That reproduces draw_line_full's loop exactly (tests/test_arith.py checks
+// it against the loop over every |dx|, |dy| <= 130), so each pixel gets the t, colour, depth,
+// texel and fog of the step that writes it.
+__device__ __noinline__ PixelOut shade_prim(const TileArgs &A, const float *r, int px, int py, uint32_t col, float dep)
+{
+    PixelOut none{col, dep, 0u};
+    if (px < __float_as_int(r[R_MINX]) || px > __float_as_int(r[R_MAXX]) || py < __float_as_int(r[R_MINY]) ||
+        py > __float_as_int(r[R_MAXY]))
+        return none;
+    const DevRaster &R = A.rasters[min(__float_as_uint(r[R_RASTER]), A.nrasters - 1)];
+    const mtgl_raster_state &rs = R.rs;
+    if (rec_type(r) == REC_POINT)
+        return point_ops(rs, r[R_Z0], make_float4(r[R_C0], r[R_C0 + 1], r[R_C0 + 2], r[R_C0 + 3]), col, dep);
+
+    const int64_t x0 = __float_as_int(r[R_X0]), y0 = __float_as_int(r[R_Y0]);
+    const int64_t x1 = __float_as_int(r[R_X1]), y1 = __float_as_int(r[R_Y1]);
+    const int64_t lw = __float_as_int(r[R_X2]), half = lw / 2;
+    const int64_t dx = x1 - x0, dy = y1 - y0;
+    const int64_t adx = dx < 0 ? -dx : dx, ady = dy < 0 ? -dy : dy;
+    const int64_t sx = dx < 0 ? -1 : 1, sy = dy < 0 ? -1 : 1;
+    int64_t k, across;
+    if (adx > ady) {
+        k = ((int64_t)px - x0) * sx;
+        if (k < 0 || k > adx) return none;
+        across = (int64_t)py - (y0 + sy * ((2 * ady * k + adx - 1) / (2 * adx)));
+    } else if (ady > 0) {
+        k = ((int64_t)py - y0) * sy;
+        if (k < 0 || k > ady) return none;
+        across = (int64_t)px - (x0 + sx * ((2 * adx * k + ady - 1) / (2 * ady)));
+    } else {
+        if (py != y0) return none;
+        k = 0;
+        across = (int64_t)px - x0;
+    }
+    if (across < -half || across >= lw - half) return none;
+    const int32_t total = (int32_t)(adx > ady ? adx : ady);
+    const float t = (float)(int32_t)k / (float)(total == 0 ? 1 : total);
+    const float z = r[R_Z0] + t * (r[R_Z1] - r[R_Z0]);
+    const float depth = map_depth(R, z);
+    float4 c = lerp_col(make_float4(r[R_C0], r[R_C0 + 1], r[R_C0 + 2], r[R_C0 + 3]),
+                        make_float4(r[R_C1], r[R_C1 + 1], r[R_C1 + 2], r[R_C1 + 3]), t);
+    if (R.tex) {
+        const float u = r[R_UV0] + t * (r[R_UV1] - r[R_UV0]);
+        const float v = r[R_UV0 + 1] + t * (r[R_UV1 + 1] - r[R_UV0 + 1]);
+        const float4 tc = unpack_rgba(sample_lod(R, u, v, 0.0f));
+        // the reference never leaves its loop when this test fails (raster.c:175, 183 skip the
+        // Bresenham step); here the pixel is dropped
+        if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) return none;
+        c = make_float4(c.x * tc.x, c.y * tc.y, c.z * tc.z, c.w * tc.w);
+    } else if (rs.alpha_test && !cmp_pass(rs.alpha_func, c.w, rs.alpha_ref)) {
+        return none;
+    }
+    if (rs.fog) c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, -(r[R_EZ0] + t * (r[R_EZ1] - r[R_EZ0]))));
+    return point_ops(rs, depth, c, col, dep);
+}
+
 // Without per-fragment lighting the kernel fits 48 registers: ask for 1280 resident
 // threads per SM (5 CTAs of 16x16, 20 of 8x8); with it, 64 registers and 1024 threads. A
 // 32x32 CTA is 1024 threads on its own.
@@ -296,8 +380,17 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                     const float dmin = r[R_DMIN];
                     if (zc == ZC_NEVER || dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)) continue;
                 }
-                const bool wrote = shade_pixel<TEX, EYE>(A, r, reinterpret_cast<const float *>(s_eye[EYE ? j : 0]),
-                                                         have_eye, px, py, fpx, fpy, col, dep, st, frags);
+                bool wrote;
+                if (rec_type(r) == REC_TRI) {
+                    wrote = shade_pixel<TEX, EYE>(A, r, reinterpret_cast<const float *>(s_eye[EYE ? j : 0]), have_eye,
+                                                  px, py, fpx, fpy, col, dep, st, frags);
+                } else {
+                    const PixelOut po = shade_prim(A, r, px, py, col, dep);
+                    col = po.col;
+                    dep = po.dep;
+                    frags += po.flags & 1u;
+                    wrote = (po.flags & 2u) != 0;
+                }
                 if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
             }
         }

@@ -51,6 +51,17 @@ enum ZCull { ZC_NONE = 0, ZC_LESS = 1, ZC_LEQUAL = 2, ZC_NEVER = 3 };
 // GL_GEQUAL, GL_NOTEQUAL or GL_ALWAYS); a warp's max depth taken before it is then no bound.
 constexpr uint32_t kFlagRaisesDepth = 8u;
 
+// R_FLAGS bits 4-5: what the record draws. Points and lines reuse the record's words:
+//   REC_POINT (draw_points / draw_point_at_screen, raster.c:777-844, 1020-1164): a square
+//     R_MINX..R_MAXY (already clamped to the framebuffer and scissor) of one depth R_Z0 and
+//     one final colour R_C0 (texture, alpha test and fog applied at setup);
+//   REC_LINE (draw_line_full, raster.c:107-241): int endpoints R_X0,R_Y0 / R_X1,R_Y1, width
+//     R_X2 (int), NDC z R_Z0/R_Z1, colours R_C0/R_C1, uv R_UV0/R_UV1, eye z R_EZ0/R_EZ1,
+//     bbox R_MINX..R_MAXY over the widened line clamped to framebuffer and scissor.
+enum RecType { REC_TRI = 0, REC_POINT = 1, REC_LINE = 2 };
+constexpr int kRecTypeShift = 4;
+__device__ __forceinline__ uint32_t rec_type(const float *r) { return (__float_as_uint(r[R_FLAGS]) >> kRecTypeShift) & 3u; }
+
 // Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).
 struct __align__(16) PostVertex {
     float4 clip;

@@ -622,6 +622,104 @@ def sc_depth_mix():
     return s
 
 
+def _line_batch(s, rng, mode, n, spread=3.0, z=(-6.0, 0.5), uv=False):
+    s.glBegin(mode)
+    for _ in range(n):
+        c = rng.uniform(0, 1, 4)
+        c[3] = rng.uniform(0.3, 1.0)
+        s.glColor4f(*map(float, c))
+        if uv:
+            s.glTexCoord2f(*map(float, rng.uniform(-1.0, 2.0, 2)))
+        p = rng.uniform(-spread, spread, 3)
+        p[2] = rng.uniform(*z)
+        s.glVertex3f(*map(float, p))
+    s.glEnd()
+
+
+def sc_lines_states():
+    """Lines of widths 1-6 in all three line modes through depth test and writes, blending,
+    linear fog and a scissor box; endpoints beyond every clip plane (near included), so
+    clip_line cuts most segments."""
+    s = base("lines_states", 96, 72)
+    rng = np.random.default_rng(37)
+    s.glEnable(G.GL_DEPTH_TEST)
+    s.glEnable(G.GL_FOG)
+    s.glFogi(G.GL_FOG_MODE, G.GL_LINEAR)
+    s.glFogf(G.GL_FOG_START, 1.0)
+    s.glFogf(G.GL_FOG_END, 9.0)
+    s.glFogfv(G.GL_FOG_COLOR, f32(0.6, 0.2, 0.1, 1.0))
+    rand_tris(s, rng, 6, spread=2.0, z=(-5.0, -2.0))
+    for i, (mode, width) in enumerate(((G.GL_LINES, 1.0), (G.GL_LINE_STRIP, 2.0), (G.GL_LINE_LOOP, 3.0),
+                                       (G.GL_LINES, 6.0), (G.GL_LINE_STRIP, 1.4), (G.GL_LINE_LOOP, 4.6))):
+        s.glLineWidth(width)
+        if i == 3:
+            s.glEnable(G.GL_BLEND)
+            s.glBlendFunc(G.GL_SRC_ALPHA, G.GL_ONE_MINUS_SRC_ALPHA)
+        if i == 4:
+            s.glEnable(G.GL_SCISSOR_TEST)
+            s.glScissor(10, 8, 60, 40)
+            s.glDepthFunc(G.GL_LEQUAL)
+            s.glDepthMask(0)
+        _line_batch(s, rng, mode, 10, spread=4.0, z=(-9.0, 1.0))
+    return s
+
+
+def sc_points_states():
+    """Points of sizes 1-6 (odd and even squares) through a texture sampled at lod 0 with
+    the alpha test on its alpha, EXP fog, blending and the depth test, near every edge."""
+    s = base("points_states", 96, 72)
+    rng = np.random.default_rng(38)
+    checker_texture(s, 8, alpha_ramp=True)
+    s.glTexEnvi(G.GL_TEXTURE_ENV, G.GL_TEXTURE_ENV_MODE, G.GL_MODULATE)
+    s.glEnable(G.GL_DEPTH_TEST)
+    s.glEnable(G.GL_FOG)
+    s.glFogi(G.GL_FOG_MODE, G.GL_EXP)
+    s.glFogf(G.GL_FOG_DENSITY, 0.2)
+    rand_tris(s, rng, 4, spread=2.0, z=(-5.0, -2.0))
+    for i, size in enumerate((1.0, 2.0, 3.0, 4.4, 6.0)):
+        s.glPointSize(size)
+        if i == 1:
+            s.glEnable(G.GL_TEXTURE_2D)
+            s.glEnable(G.GL_ALPHA_TEST)
+            s.glAlphaFunc(G.GL_GREATER, 0.3)
+        if i == 3:
+            s.glEnable(G.GL_BLEND)
+            s.glBlendFunc(G.GL_ONE, G.GL_ONE)
+        _line_batch(s, rng, G.GL_POINTS, 40, spread=3.2, z=(-8.0, 0.5), uv=True)
+    s.glDisable(G.GL_TEXTURE_2D)
+    s.glPointSize(2.0)
+    _line_batch(s, rng, G.GL_POINTS, 30, spread=3.2, z=(-8.0, 0.5))  # alpha test on the colour
+    return s
+
+
+def sc_polygon_modes_lit():
+    """glPolygonMode LINE on front faces and POINT on back faces under GL_PHONG lighting
+    (vertex colours lit per vertex), a bound texture (lines sample it, points do not), fog and
+    wide lines, on triangles that the near and side planes clip."""
+    s = base("polygon_modes_lit", 96, 72)
+    rng = np.random.default_rng(39)
+    checker_texture(s, 8)
+    s.glEnable(G.GL_TEXTURE_2D)
+    s.glEnable(G.GL_DEPTH_TEST)
+    s.glEnable(G.GL_LIGHTING)
+    s.glEnable(G.GL_LIGHT0)
+    s.glLightfv(G.GL_LIGHT0, G.GL_POSITION, f32(1.0, 2.0, 2.0, 0.0))
+    s.glShadeModel(G.GL_PHONG)
+    s.glEnable(G.GL_FOG)
+    s.glFogi(G.GL_FOG_MODE, G.GL_EXP2)
+    s.glFogf(G.GL_FOG_DENSITY, 0.12)
+    s.glPolygonMode(G.GL_FRONT, G.GL_LINE)
+    s.glPolygonMode(G.GL_BACK, G.GL_POINT)
+    s.glLineWidth(2.0)
+    s.glTranslatef(0.0, 0.0, -3.0)
+    rand_tris(s, rng, 12, spread=2.5, z=(-3.0, 3.5), uv=True, normal=True)
+    s.glShadeModel(G.GL_SMOOTH)
+    s.glPolygonMode(G.GL_FRONT_AND_BACK, G.GL_LINE)
+    s.glLineWidth(1.0)
+    rand_tris(s, rng, 8, spread=2.5, z=(-3.0, 3.5), uv=True, normal=True)
+    return s
+
+
 SCENES = {
     "clip_big": (sc_clip_big, ()),
     "clip_near_far": (sc_clip_near_far, ()),
@@ -655,4 +753,7 @@ SCENES = {
     "phong_textured_fog": (sc_phong_textured_fog, ()),
     "texture_matrix": (sc_texture_matrix, ()),
     "depth_mix": (sc_depth_mix, ()),
+    "lines_states": (sc_lines_states, ("lines",)),
+    "points_states": (sc_points_states, ("lines",)),
+    "polygon_modes_lit": (sc_polygon_modes_lit, ("lines",)),
 }

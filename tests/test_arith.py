@@ -65,3 +65,41 @@ def test_texel_wrap_shortcuts_match_reference_rule():
             if x + 1 < 2**31:
                 nxt = 0 if fast + 1 == n else fast + 1
                 assert nxt == _c_mod(_c_mod(x + 1, n) + n, n), (x, n)
+
+
+def _bresenham(x0, y0, x1, y1):
+    """draw_line_full's pixel loop (raster.c:107-241), positions only."""
+    dx, dy = x1 - x0, y1 - y0
+    adx, ady = abs(dx), abs(dy)
+    sx, sy = (-1 if dx < 0 else 1), (-1 if dy < 0 else 1)
+    err, cx, cy, out = adx - ady, x0, y0, []
+    while True:
+        out.append((cx, cy))
+        if cx == x1 and cy == y1:
+            return out
+        e2 = 2 * err
+        if e2 > -ady:
+            err -= ady
+            cx += sx
+        if e2 < adx:
+            err += adx
+            cy += sy
+
+
+def test_line_step_closed_form_matches_the_loop():
+    """The tile kernel's closed form of the Bresenham step (shade_prim) against the loop."""
+    n = 130
+    for dx in range(-n, n + 1):
+        for dy in range(-n, n + 1, 1 if abs(dx) < 20 else 7):
+            pts = _bresenham(3, -5, 3 + dx, -5 + dy)
+            adx, ady = abs(dx), abs(dy)
+            sx, sy = (-1 if dx < 0 else 1), (-1 if dy < 0 else 1)
+            assert len(pts) == max(adx, ady) + 1
+            for k, (cx, cy) in enumerate(pts):
+                if adx > ady:
+                    want = (3 + sx * k, -5 + sy * ((2 * ady * k + adx - 1) // (2 * adx)))
+                elif ady > 0:
+                    want = (3 + sx * ((2 * adx * k + ady - 1) // (2 * ady)), -5 + sy * k)
+                else:
+                    want = (3, -5)
+                assert (cx, cy) == want, (dx, dy, k)

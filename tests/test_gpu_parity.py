@@ -15,8 +15,7 @@ from mytinygl_gb300.scene import Scene, render
 
 pytestmark = pytest.mark.gpu
 
-TRI_SCENES = sorted(n for n, (b, flags) in F.SCENES.items() if "lines" not in flags)
-LINE_SCENES = sorted(n for n, (b, flags) in F.SCENES.items() if "lines" in flags)
+ALL_SCENES = sorted(F.SCENES)
 
 
 @pytest.fixture(scope="module")
@@ -37,14 +36,12 @@ def check(gpu, oracle, scene, tol=1):
     return stats
 
 
-@pytest.mark.parametrize("name", TRI_SCENES)
+@pytest.mark.parametrize("name", ALL_SCENES)
 def test_feature_scene(gpu, oracle, name):
     check(gpu, oracle, F.SCENES[name][0]())
 
 
-@pytest.mark.parametrize("path", [p for p in harness.golden_files()
-                                  if not any(p.endswith(f"/{n}.npz") for n in LINE_SCENES)],
-                         ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+@pytest.mark.parametrize("path", harness.golden_files(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
 def test_golden(gpu, path):
     scene, expected, buffers = harness.load_golden(path)
     stats = harness.compare(expected, render(gpu, scene), buffers)
@@ -129,13 +126,31 @@ def test_readpixels(gpu, oracle):
     assert d.max() <= 1
 
 
-@pytest.mark.parametrize("name", LINE_SCENES)
-def test_points_and_lines_are_reported(gpu, name):
-    """Points, lines and glPolygonMode POINT/LINE have no kernel yet: the draw is refused
-    with GL_INVALID_OPERATION instead of rendering something different."""
-    scene = F.SCENES[name][0]()
-    c, d, s, err = render(gpu, scene)
-    assert err == G.GL_INVALID_OPERATION
+def test_random_points_and_lines(gpu, oracle):
+    """Seeded mixes of points and lines of every mode and width with triangles, through
+    random depth, blend, fog, texture and scissor states."""
+    for seed in range(6):
+        rng = np.random.default_rng(500 + seed)
+        s = Scene(f"points_lines_{seed}", 80, 60)
+        s.glViewport(0, 0, 80, 60)
+        s.glClearColor(0.1, 0.1, 0.1, 1.0)
+        s.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT | G.GL_STENCIL_BUFFER_BIT)
+        s.glMatrixMode(G.GL_PROJECTION)
+        s.glFrustum(*W.frustum_params(60.0, 80 / 60, 0.5, 20.0))
+        s.glMatrixMode(G.GL_MODELVIEW)
+        s.glTranslatef(0.0, 0.0, -4.0)
+        F.checker_texture(s, 8)
+        for _ in range(8):
+            s.glDepthFunc([G.GL_LESS, G.GL_LEQUAL, G.GL_GREATER, G.GL_ALWAYS][int(rng.integers(0, 4))])
+            for cap in (G.GL_DEPTH_TEST, G.GL_BLEND, G.GL_FOG, G.GL_TEXTURE_2D, G.GL_SCISSOR_TEST):
+                (s.glEnable if rng.uniform() < 0.5 else s.glDisable)(cap)
+            s.glBlendFunc(G.GL_SRC_ALPHA, G.GL_ONE_MINUS_SRC_ALPHA)
+            s.glScissor(int(rng.integers(0, 30)), int(rng.integers(0, 20)), 50, 40)
+            s.glLineWidth(float(rng.uniform(0.5, 5.0)))
+            s.glPointSize(float(rng.uniform(0.5, 5.0)))
+            mode = [G.GL_POINTS, G.GL_LINES, G.GL_LINE_STRIP, G.GL_LINE_LOOP, G.GL_TRIANGLES][int(rng.integers(0, 5))]
+            F._line_batch(s, rng, mode, 12, spread=3.0, z=(-5.0, 3.0), uv=True)
+        check(gpu, oracle, s)
 
 
 @pytest.mark.parametrize("which", ["textured", "zbuffer", "depth_range", "clip_big", "stencil", "mipmap_floor",

@@ -21,7 +21,7 @@
 
 namespace mtgl {
 
-constexpr int kChunk = 32;  // records staged per step: one per lane for the overlap ballot
+constexpr int kChunk = 32;  // records tested per step: one per lane for the overlap ballot
 
 __device__ __forceinline__ bool covers_tile(const ClearOp &c, uint32_t bit, int x0, int y0, int x1, int y1)
 {
@@ -46,7 +46,8 @@ __device__ __forceinline__ float warp_max_depth(float dep, bool in_fb)
 // thread's pixel. Returns true when it wrote the depth buffer. TEX / EYE compile the
 // texturing and per-fragment lighting stages in only for passes that use them.
 template <bool TEX, bool EYE>
-__device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *r, const float *e, bool have_eye, int px,
+__device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__restrict__ r, const float *__restrict__ e,
+                                            bool have_eye, int px,
                                             int py, float fpx, float fpy, uint32_t &col, float &dep, uint32_t &st,
                                             uint32_t &frags)
 {
@@ -249,8 +250,6 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
 {
     constexpr int kThreads = TS * TS;
     constexpr int kWarpsX = TS / 8;  // 8x4-pixel warp blocks per tile row band
-    __shared__ float4 s_rec[kChunk][kRecWords / 4];
-    __shared__ float4 s_eye[EYE ? kChunk : 1][kEyeWords / 4];
     __shared__ uint32_t s_tile, s_frame;
 
     if (A.guard && (A.guard[0] > A.records_cap || A.guard[1] > A.pairs_cap)) return;
@@ -330,60 +329,52 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
         // hierarchical z: the warp's largest stored depth, refreshed whenever the warp writes depth
         float wzmax = warp_max_depth(dep, in_fb);
 
+        // Each warp walks the tile's list on its own: no barrier between warps, which differ
+        // in how many records meet their 8x4 block. Record words are read through L1 with
+        // all lanes on one address (a broadcast); the CTA's warps share those lines.
+        const float4 *recs4 = reinterpret_cast<const float4 *>(A.records);
         for (uint32_t base = 0; base < count; base += kChunk) {
             const int n = (int)min((uint32_t)kChunk, count - base);
-            __syncthreads();
-            for (int i = threadIdx.x; i < n * (kRecWords / 4); i += kThreads) {
-                const int r = i / (kRecWords / 4), q = i % (kRecWords / 4);
-                const uint32_t idx = __ldg(A.tile_vals + start + base + r);
-                s_rec[r][q] = __ldg(reinterpret_cast<const float4 *>(A.records) + (size_t)idx * (kRecWords / 4) + q);
-            }
-            if (have_eye) {
-                for (int i = threadIdx.x; i < n * (kEyeWords / 4); i += kThreads) {
-                    const int r = i / (kEyeWords / 4), q = i % (kEyeWords / 4);
-                    const uint32_t idx = __ldg(A.tile_vals + start + base + r);
-                    s_eye[r][q] =
-                        __ldg(reinterpret_cast<const float4 *>(A.eye_records) + (size_t)idx * (kEyeWords / 4) + q);
-                }
-            }
-            __syncthreads();
-
-            // Lane j tests staged record j against the warp: its bbox must meet the warp's block,
-            // and the depth rejection is tried with the warp's max depth as of now. That value is
-            // still an upper bound when record j is reached unless an earlier record of the chunk
-            // may raise depths, so rejection is only taken when none before j can. The set bits,
-            // lowest first, are this warp's records of the chunk in submission order.
+            // Lane j tests record base+j against the warp: its bbox must meet the warp's block,
+            // and the depth rejection is tried with the warp's max depth as of now. That value
+            // is still an upper bound when record j is reached unless an earlier record of the
+            // step may raise depths, so rejection is only taken when none before j can. The set
+            // bits, lowest first, are this warp's records of the step in submission order.
+            uint32_t idx = 0, flags = 0;
+            float dmin = 0.0f;
             bool take = false;
-            uint32_t raises = 0;
             if (lane < n) {
-                const float4 bb = s_rec[lane][1], bb2 = s_rec[lane][2];
+                idx = __ldg(A.tile_vals + start + base + lane);
+                const float4 *q = recs4 + (size_t)idx * (kRecWords / 4);
+                const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2);
                 take = !(__float_as_int(bb2.x) < wx0 || __float_as_int(bb.z) > wx0 + 7 ||
                          __float_as_int(bb2.y) < wy0 || __float_as_int(bb.w) > wy0 + 3);
-                raises = __float_as_uint(reinterpret_cast<const float *>(s_rec[lane])[R_FLAGS]) & kFlagRaisesDepth;
+                flags = __float_as_uint(__ldg(reinterpret_cast<const float *>(q) + R_FLAGS));
+                dmin = __ldg(reinterpret_cast<const float *>(q) + R_DMIN);
             }
-            const uint32_t raise_mask = __ballot_sync(0xffffffffu, raises != 0);
+            const uint32_t raise_mask = __ballot_sync(0xffffffffu, (flags & kFlagRaisesDepth) != 0);
+            const uint32_t zc_l = (flags >> 1) & 3u;
             if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
-                const float *rl = reinterpret_cast<const float *>(s_rec[lane]);
-                const uint32_t zc = (__float_as_uint(rl[R_FLAGS]) >> 1) & 3u;
-                const float dmin = rl[R_DMIN];
-                if (zc == ZC_NEVER || (zc != ZC_NONE && (dmin > wzmax || (zc == ZC_LESS && dmin == wzmax))))
+                if (zc_l == ZC_NEVER || (zc_l != ZC_NONE && (dmin > wzmax || (zc_l == ZC_LESS && dmin == wzmax))))
                     take = false;
             }
             uint32_t todo = __ballot_sync(0xffffffffu, take);
             while (todo) {
                 const int j = __ffs(todo) - 1;
                 todo &= todo - 1;
-                const float *r = reinterpret_cast<const float *>(s_rec[j]);
+                const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                const float rdmin = __shfl_sync(0xffffffffu, dmin, j);
                 // warp-uniform rejection: no fragment of this triangle can pass the depth test here
-                const uint32_t zc = (__float_as_uint(r[R_FLAGS]) >> 1) & 3u;
+                const uint32_t zc = (rflags >> 1) & 3u;
                 if (zc != ZC_NONE) {
-                    const float dmin = r[R_DMIN];
-                    if (zc == ZC_NEVER || dmin > wzmax || (zc == ZC_LESS && dmin == wzmax)) continue;
+                    if (zc == ZC_NEVER || rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax)) continue;
                 }
+                const float *r = A.records + (size_t)ridx * kRecWords;
                 bool wrote;
-                if (rec_type(r) == REC_TRI) {
-                    wrote = shade_pixel<TEX, EYE>(A, r, reinterpret_cast<const float *>(s_eye[EYE ? j : 0]), have_eye,
-                                                  px, py, fpx, fpy, col, dep, st, frags);
+                if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {
+                    const float *e = have_eye ? A.eye_records + (size_t)ridx * kEyeWords : nullptr;
+                    wrote = shade_pixel<TEX, EYE>(A, r, e, have_eye, px, py, fpx, fpy, col, dep, st, frags);
                 } else {
                     const PixelOut po = shade_prim(A, r, px, py, col, dep);
                     col = po.col;

@@ -75,7 +75,7 @@ struct Pass {
 enum ScratchSlot {
     S_VERTS, S_EYES, S_TRI_COUNTS, S_TRI_OFFSETS, S_RECORDS, S_EYE_RECORDS, S_REC_TILES, S_KEYS, S_VALS,
     S_KEYS_ALT, S_VALS_ALT, S_TILE_COUNT, S_TILE_START, S_RADIX_HIST, S_SCAN_TEMP, S_ORDER, S_ORDER_AUX,
-    kScratchSlots
+    S_CLIP_LIST, kScratchSlots
 };
 
 struct ScratchSource {
@@ -110,7 +110,7 @@ struct Exec {
     PoolScratch pool;
     uint8_t *dstage = nullptr;
     size_t dcap = 0;
-    uint32_t *d_totals = nullptr;  // [0] records, [1] pairs, [2] tiles' records, [3] sort scratch
+    uint32_t *d_totals = nullptr;  // [0] records, [1] pairs, [2] tiles' records, [3] sort scratch, [4] clip list
     uint32_t *h_totals = nullptr;  // pinned copy of [0..1]
     unsigned long long *d_frags = nullptr;
     // per-phase profiling: 5 events per pass (before K1, after K1, after K2, after K3, after K4)

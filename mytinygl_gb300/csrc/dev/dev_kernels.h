@@ -26,6 +26,9 @@ struct GeomArgs {
     float *records;                   // emit pass output, kRecWords per record
     float *eye_records;               // emit pass output, kEyeWords per record (may be null)
     uint32_t records_cap;             // records the output buffers hold (writes beyond are dropped)
+    uint32_t *clip_list;              // triangles that straddle a clip plane (total_tris entries)
+    uint32_t *clip_count;             // their number (device; zeroed by the count launch)
+    int32_t sms;
 };
 
 // K1: per-vertex stage (gl_api.c:263-348) for every vertex slot of the pass.

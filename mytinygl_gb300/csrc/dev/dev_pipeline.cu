@@ -337,6 +337,8 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if (eye && (rc = sc.take(S_EYES, slots, &eyes))) return rc;
     if ((rc = sc.take(S_TRI_COUNTS, tris, &tri_counts))) return rc;
     if ((rc = sc.take(S_TRI_OFFSETS, tris, &tri_offsets))) return rc;
+    uint32_t *clip_list = nullptr;
+    if ((rc = sc.take(S_CLIP_LIST, tris, &clip_list))) return rc;
     if ((rc = sc.take(S_TILE_COUNT, (size_t)ntiles + 1, &tile_count))) return rc;
     if ((rc = sc.take(S_TILE_START, (size_t)ntiles + 1, &tile_start))) return rc;
     if (c.ctas && c.order && (rc = sc.take(S_ORDER, ntiles, &order))) return rc;
@@ -376,6 +378,9 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ga.total_tris = tris;
     ga.tri_counts = tri_counts;
     ga.tri_offsets = tri_offsets;
+    ga.clip_list = clip_list;
+    ga.clip_count = x.d_totals + 4;
+    ga.sms = x.sms;
     int launches = 0;
     launches += launch_vertex(ga, s);
     x.prof_mark();

@@ -8,6 +8,8 @@
 // culling (raster.c:751-774, 901-958) and the per-triangle part of
 // rasterize_triangle_smooth (raster.c:458-529). The count pass sizes the output; after an
 // exclusive scan the emit pass writes each record at its submission-order position.
+#include <algorithm>
+
 #include "dev_kernels.h"
 
 namespace mtgl {
@@ -157,25 +159,47 @@ __global__ void __launch_bounds__(128) k_vertex(GeomArgs A)
 
 // ------------------------------------------------------------------ K2
 
-struct CV {
+// A vertex through clipping: clip position, colour, uv, eye z and, only in passes that
+// light per fragment, the eye position and normal (elsewhere they are the constants the
+// vertex stage leaves, (0,0,0) and (0,0,1), which every lerp keeps).
+template <bool EYE>
+struct CVx;
+template <>
+struct CVx<true> {
     float4 clip;
     float4 col;
     float2 uv;
     float ez;
     float3 ep, en;
 };
+template <>
+struct CVx<false> {
+    float4 clip;
+    float4 col;
+    float2 uv;
+    float ez;
+};
+__device__ __forceinline__ float3 cv_ep(const CVx<true> &v) { return v.ep; }
+__device__ __forceinline__ float3 cv_en(const CVx<true> &v) { return v.en; }
+__device__ __forceinline__ float3 cv_ep(const CVx<false> &) { return make_float3(0.0f, 0.0f, 0.0f); }
+__device__ __forceinline__ float3 cv_en(const CVx<false> &) { return make_float3(0.0f, 0.0f, 1.0f); }
 
 // vertex_lerp (graphics.h:465-475): colour uses a*(1-t)+b*t, the rest a+t*(b-a)
-__device__ __forceinline__ CV cv_lerp(const CV &a, const CV &b, float t)
+template <bool EYE>
+__device__ __forceinline__ CVx<EYE> cv_lerp(const CVx<EYE> &a, const CVx<EYE> &b, float t)
 {
-    CV v;
+    CVx<EYE> v;
     v.clip = make_float4(a.clip.x + t * (b.clip.x - a.clip.x), a.clip.y + t * (b.clip.y - a.clip.y),
                          a.clip.z + t * (b.clip.z - a.clip.z), a.clip.w + t * (b.clip.w - a.clip.w));
     v.col = lerp_col(a.col, b.col, t);
     v.uv = make_float2(a.uv.x + t * (b.uv.x - a.uv.x), a.uv.y + t * (b.uv.y - a.uv.y));
     v.ez = a.ez + t * (b.ez - a.ez);
-    v.ep = make_float3(a.ep.x + t * (b.ep.x - a.ep.x), a.ep.y + t * (b.ep.y - a.ep.y), a.ep.z + t * (b.ep.z - a.ep.z));
-    v.en = make_float3(a.en.x + t * (b.en.x - a.en.x), a.en.y + t * (b.en.y - a.en.y), a.en.z + t * (b.en.z - a.en.z));
+    if constexpr (EYE) {
+        v.ep = make_float3(a.ep.x + t * (b.ep.x - a.ep.x), a.ep.y + t * (b.ep.y - a.ep.y),
+                           a.ep.z + t * (b.ep.z - a.ep.z));
+        v.en = make_float3(a.en.x + t * (b.en.x - a.en.x), a.en.y + t * (b.en.y - a.en.y),
+                           a.en.z + t * (b.en.z - a.en.z));
+    }
     return v;
 }
 
@@ -191,7 +215,8 @@ __device__ __forceinline__ float plane_dist(const float4 &v, int p)
     }
 }
 
-__device__ __forceinline__ void snap_plane(CV &v, int p)
+template <class V>
+__device__ __forceinline__ void snap_plane(V &v, int p)
 {
     switch (p) {
     case 2: v.clip.x = -v.clip.w; break;
@@ -226,16 +251,17 @@ __device__ __forceinline__ int clip_start(const float4 &a, const float4 &b, cons
 
 // clip_triangle (clipping.h:106-126): Sutherland-Hodgman passes from plane `first` on (the
 // earlier ones copy the triangle unchanged, see clip_start); result in bufA[0..n)
-__device__ __noinline__ int clip_triangle(CV *bufA, CV *bufB, int first)
+template <class V>
+__device__ __noinline__ int clip_triangle(V *bufA, V *bufB, int first)
 {
     int n = 3;
-    CV *in = bufA, *out = bufB;
+    V *in = bufA, *out = bufB;
     for (int p = first; p < 6; p++) {
         int m = 0;
-        const CV *prev = &in[n - 1];
+        const V *prev = &in[n - 1];
         float pd = plane_dist(prev->clip, p);
         for (int i = 0; i < n; i++) {
-            const CV *cur = &in[i];
+            const V *cur = &in[i];
             float cd = plane_dist(cur->clip, p);
             if (pd >= 0) {
                 if (cd >= 0) {
@@ -261,7 +287,7 @@ __device__ __noinline__ int clip_triangle(CV *bufA, CV *bufB, int first)
             pd = cd;
         }
         n = m;
-        CV *tmp = in;
+        V *tmp = in;
         in = out;
         out = tmp;
         if (n == 0) return 0;
@@ -272,7 +298,8 @@ __device__ __noinline__ int clip_triangle(CV *bufA, CV *bufB, int first)
     return n;
 }
 
-__device__ __forceinline__ void persp_divide(CV &v)
+template <class V>
+__device__ __forceinline__ void persp_divide(V &v)
 {
     if (fabsf(v.clip.w) < 1e-6f) {
         v.clip = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
@@ -342,20 +369,18 @@ __device__ __forceinline__ uint32_t element_slot(const DevDraw &D, uint32_t e)
     return D.vslot_base + (uint32_t)rel;
 }
 
-__device__ __forceinline__ void load_cv(const GeomArgs &A, uint32_t slot, bool eye, CV &v)
+template <bool EYE>
+__device__ __forceinline__ void load_cv(const GeomArgs &A, uint32_t slot, CVx<EYE> &v)
 {
     const PostVertex pv = A.verts[slot];
     v.clip = pv.clip;
     v.col = pv.color;
     v.uv = pv.uv;
     v.ez = pv.eye_z;
-    if (eye) {
+    if constexpr (EYE) {
         const PostEye e = A.eyes[slot];
         v.ep = make_float3(e.pos_nx.x, e.pos_nx.y, e.pos_nx.z);
         v.en = make_float3(e.pos_nx.w, e.nyz.x, e.nyz.y);
-    } else {
-        v.ep = make_float3(0.0f, 0.0f, 0.0f);
-        v.en = make_float3(0.0f, 0.0f, 1.0f);
     }
 }
 
@@ -470,8 +495,9 @@ __device__ __forceinline__ uint32_t screen_point(const DevRaster &R, uint32_t ra
 // flush_points' per-vertex part (raster.c:1020-1164): clip-volume test, divide, screen
 // position, texture at lod 0 with the alpha test on its alpha (else on the colour), fog,
 // and the point_size square.
+template <class V>
 __device__ __forceinline__ uint32_t vertex_point(const DevRaster &R, uint32_t raster_id, uint32_t frame,
-                                                 const FrameDims &dims, const CV &v, float *rec)
+                                                 const FrameDims &dims, const V &v, float *rec)
 {
     const mtgl_raster_state &rs = R.rs;
     const float4 p = v.clip;
@@ -550,7 +576,8 @@ __device__ __forceinline__ int outcode(const float4 &v)
     return c;
 }
 
-__device__ bool clip_line(CV &a, CV &b)
+template <class V>
+__device__ bool clip_line(V &a, V &b)
 {
     int ca = outcode(a.clip), cb = outcode(b.clip);
     for (int round = 0; round < 32; round++) {
@@ -568,7 +595,7 @@ __device__ bool clip_line(CV &a, CV &b)
         else { d0 = p0.w - p0.z; d1 = p1.w - p1.z; plane = 1; }
         const float denom = d0 - d1;
         if (fabsf(denom) < 1e-10f) return false;
-        CV cl = cv_lerp(a, b, d0 / denom);
+        V cl = cv_lerp(a, b, d0 / denom);
         snap_plane(cl, plane);
         if (co == ca) {
             a = cl;
@@ -582,8 +609,9 @@ __device__ bool clip_line(CV &a, CV &b)
 }
 
 // draw_line_segment (raster.c:244-285): clip, divide (|w| < 1e-6 maps to the origin), screen.
-__device__ uint32_t segment_line(const DevRaster &R, uint32_t raster_id, uint32_t frame, const FrameDims &dims, CV a,
-                                 CV b, float *rec)
+template <class V>
+__device__ uint32_t segment_line(const DevRaster &R, uint32_t raster_id, uint32_t frame, const FrameDims &dims, V a,
+                                 V b, float *rec)
 {
     if (!clip_line(a, b)) return 0;
     float z0, z1;
@@ -630,8 +658,9 @@ struct RecOut {
 
 // Per fan triangle: the setup half of rasterize_triangle_smooth. Returns true when the
 // triangle produces a record; writes it when `rec` is non-null.
+template <class V>
 __device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t raster_id, uint32_t frame,
-                                                  const FrameDims &dims, const CV &a, const CV &b, const CV &c,
+                                                  const FrameDims &dims, const V &a, const V &b, const V &c,
                                                   const RecOut &o, uint32_t at)
 {
     const mtgl_raster_state &rs = R.rs;
@@ -648,9 +677,9 @@ __device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t r
         // under GL_PHONG (phong_vertex_colors), then three points or three edges
         float4 c0 = a.col, c1 = b.col, c2 = c.col;
         if (rs.lighting && rs.shade_model == GL_PHONG) {
-            c0 = compute_lighting(rs.lit, a.ep, a.en, rs.lit.front);
-            c1 = compute_lighting(rs.lit, b.ep, b.en, rs.lit.front);
-            c2 = compute_lighting(rs.lit, c.ep, c.en, rs.lit.front);
+            c0 = compute_lighting(rs.lit, cv_ep(a), cv_en(a), rs.lit.front);
+            c1 = compute_lighting(rs.lit, cv_ep(b), cv_en(b), rs.lit.front);
+            c2 = compute_lighting(rs.lit, cv_ep(c), cv_en(c), rs.lit.front);
         }
         uint32_t n = 0;
         if (pm == GL_POINT) {
@@ -735,12 +764,13 @@ __device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t r
     r4[12] = make_float4(__uint_as_float(flags), fy2 - fy1, fx2 - fx1, fy0 - fy2);
     r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, __uint_as_float(frame));
     if (eyerec) {
+        const float3 aep = cv_ep(a), aen = cv_en(a), bep = cv_ep(b), ben = cv_en(b), cep = cv_ep(c), cen = cv_en(c);
         float4 *e4 = reinterpret_cast<float4 *>(eyerec);
-        e4[0] = make_float4(a.ep.x, a.ep.y, a.ep.z, a.en.x);
-        e4[1] = make_float4(a.en.y, a.en.z, b.ep.x, b.ep.y);
-        e4[2] = make_float4(b.ep.z, b.en.x, b.en.y, b.en.z);
-        e4[3] = make_float4(c.ep.x, c.ep.y, c.ep.z, c.en.x);
-        e4[4] = make_float4(c.en.y, c.en.z, 0.0f, 0.0f);
+        e4[0] = make_float4(aep.x, aep.y, aep.z, aen.x);
+        e4[1] = make_float4(aen.y, aen.z, bep.x, bep.y);
+        e4[2] = make_float4(bep.z, ben.x, ben.y, ben.z);
+        e4[3] = make_float4(cep.x, cep.y, cep.z, cen.x);
+        e4[4] = make_float4(cen.y, cen.z, 0.0f, 0.0f);
     }
     return 1;
 }
@@ -760,64 +790,118 @@ __device__ __forceinline__ void element_pair(uint32_t mode, uint32_t k, uint32_t
 // K2, one thread per primitive (a point, a line or a triangle of the draw's mode). The count
 // pass stores how many records the primitive produces; the emit pass writes them at the
 // primitive's offset (exclusive scan of the counts), so records keep submission order.
-template <bool EMIT>
+// Triangles that straddle a clip plane go to a list that k_clip handles: the clipper's
+// per-thread vertex buffers live in local memory, and keeping them off this kernel's
+// threads keeps that memory small enough to stay in cache.
+template <bool EYE>
+struct Prim {
+    const DevDraw *D;
+    const DevRaster *R;
+    uint32_t k, frame;
+    FrameDims dims;
+};
+
+template <bool EYE>
+__device__ __forceinline__ Prim<EYE> prim_of(const GeomArgs &A, uint32_t t)
+{
+    Prim<EYE> p;
+    const int d = find_base(A.draw_tri_base, A.ndraws, t);
+    p.D = &A.draws[d];
+    p.k = t - p.D->tri_base;
+    p.R = &A.rasters[p.D->raster];
+    p.frame = min(p.R->frame, A.nframes - 1);
+    p.dims = A.frames[p.frame].dims;
+    return p;
+}
+
+__device__ __forceinline__ RecOut rec_out(const GeomArgs &A, uint32_t t, bool emit, bool eye)
+{
+    RecOut o;
+    o.recs = emit ? A.records : nullptr;
+    o.eyes = (emit && eye) ? A.eye_records : nullptr;
+    o.base = emit ? A.tri_offsets[t] : 0;
+    o.cap = A.records_cap;
+    return o;
+}
+
+template <bool EMIT, bool EYE>
 __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
 {
+    using V = CVx<EYE>;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.total_tris) return;
     if (EMIT && A.tri_counts[t] == 0) return;  // the count pass found nothing to emit
-    const int d = find_base(A.draw_tri_base, A.ndraws, t);
-    const DevDraw &D = A.draws[d];
-    const uint32_t k = t - D.tri_base;
-    const DevRaster &R = A.rasters[D.raster];
-    const bool eye = R.needs_eye && A.eyes;
-    const uint32_t frame = min(R.frame, A.nframes - 1);
-    const FrameDims dims = A.frames[frame].dims;
-    RecOut o;
-    o.recs = EMIT ? A.records : nullptr;
-    o.eyes = (EMIT && eye) ? A.eye_records : nullptr;
-    o.base = EMIT ? A.tri_offsets[t] : 0;
-    o.cap = A.records_cap;
+    const Prim<EYE> P = prim_of<EYE>(A, t);
+    const DevDraw &D = *P.D;
+    const DevRaster &R = *P.R;
+    const RecOut o = rec_out(A, t, EMIT, EYE);
     uint32_t produced = 0;
 
     if (D.mode == GL_POINTS) {
-        CV v;
-        load_cv(A, element_slot(D, k), eye, v);
-        produced = vertex_point(R, D.raster, frame, dims, v, o.rec(0));
+        V v;
+        load_cv(A, element_slot(D, P.k), v);
+        produced = vertex_point(R, D.raster, P.frame, P.dims, v, o.rec(0));
     } else if (D.mode == GL_LINES || D.mode == GL_LINE_STRIP || D.mode == GL_LINE_LOOP) {
         uint32_t e0, e1;
-        element_pair(D.mode, k, (uint32_t)D.count, e0, e1);
-        CV v0, v1;
-        load_cv(A, element_slot(D, e0), eye, v0);
-        load_cv(A, element_slot(D, e1), eye, v1);
-        produced = segment_line(R, D.raster, frame, dims, v0, v1, o.rec(0));
+        element_pair(D.mode, P.k, (uint32_t)D.count, e0, e1);
+        V v0, v1;
+        load_cv(A, element_slot(D, e0), v0);
+        load_cv(A, element_slot(D, e1), v1);
+        produced = segment_line(R, D.raster, P.frame, P.dims, v0, v1, o.rec(0));
     } else {
         uint32_t e0, e1, e2;
-        element_triple(D.mode, k, e0, e1, e2);
-        CV v0, v1, v2;
-        load_cv(A, element_slot(D, e0), eye, v0);
-        load_cv(A, element_slot(D, e1), eye, v1);
-        load_cv(A, element_slot(D, e2), eye, v2);
+        element_triple(D.mode, P.k, e0, e1, e2);
+        V v0, v1, v2;
+        load_cv(A, element_slot(D, e0), v0);
+        load_cv(A, element_slot(D, e1), v1);
+        load_cv(A, element_slot(D, e2), v2);
         const int start = clip_start(v0.clip, v1.clip, v2.clip);
         if (start == kClipNone) {  // the clipper would return the triangle unchanged
             persp_divide(v0);
             persp_divide(v1);
             persp_divide(v2);
-            produced = setup_fan_tri(R, D.raster, frame, dims, v0, v1, v2, o, 0);
+            produced = setup_fan_tri(R, D.raster, P.frame, P.dims, v0, v1, v2, o, 0);
         } else if (start != kClipEmpty) {
-            CV bufA[kClipMax], bufB[kClipMax];
-            bufA[0] = v0;
-            bufA[1] = v1;
-            bufA[2] = v2;
-            const int n = clip_triangle(bufA, bufB, start);
-            if (n >= 3) {
-                for (int j = 0; j < n; j++) persp_divide(bufA[j]);
-                for (int j = 1; j + 1 < n; j++)
-                    produced += setup_fan_tri(R, D.raster, frame, dims, bufA[0], bufA[j], bufA[j + 1], o, produced);
-            }
+            if (EMIT) return;  // k_clip emits it
+            const uint32_t slot = atomicAdd(A.clip_count, 1u);
+            if (slot < A.total_tris) A.clip_list[slot] = t;
+            return;  // k_clip stores its count
         }
     }
     if (!EMIT) A.tri_counts[t] = produced;
+}
+
+// The listed triangles: Sutherland-Hodgman from the first plane that is not all-inside, then
+// the fan. Grid-strided over the list (its length is on the device), with the grid capped
+// so that the resident threads' clip buffers fit in cache.
+template <bool EMIT, bool EYE>
+__global__ void __launch_bounds__(64) k_clip(GeomArgs A)
+{
+    using V = CVx<EYE>;
+    const uint32_t n = min(*A.clip_count, A.total_tris);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t t = A.clip_list[i];
+        if (EMIT && A.tri_counts[t] == 0) continue;
+        const Prim<EYE> P = prim_of<EYE>(A, t);
+        const DevDraw &D = *P.D;
+        const DevRaster &R = *P.R;
+        const RecOut o = rec_out(A, t, EMIT, EYE);
+        uint32_t e0, e1, e2;
+        element_triple(D.mode, P.k, e0, e1, e2);
+        V bufA[kClipMax], bufB[kClipMax];
+        load_cv(A, element_slot(D, e0), bufA[0]);
+        load_cv(A, element_slot(D, e1), bufA[1]);
+        load_cv(A, element_slot(D, e2), bufA[2]);
+        const int start = clip_start(bufA[0].clip, bufA[1].clip, bufA[2].clip);
+        uint32_t produced = 0;
+        const int nv = (start < kClipNone) ? clip_triangle(bufA, bufB, start) : 0;
+        if (nv >= 3) {
+            for (int j = 0; j < nv; j++) persp_divide(bufA[j]);
+            for (int j = 1; j + 1 < nv; j++)
+                produced += setup_fan_tri(R, D.raster, P.frame, P.dims, bufA[0], bufA[j], bufA[j + 1], o, produced);
+        }
+        if (!EMIT) A.tri_counts[t] = produced;
+    }
 }
 
 int launch_vertex(const GeomArgs &a, cudaStream_t s)
@@ -827,18 +911,42 @@ int launch_vertex(const GeomArgs &a, cudaStream_t s)
     return 1;
 }
 
+namespace {
+
+unsigned clip_grid(const GeomArgs &a)
+{
+    const uint64_t want = ((uint64_t)a.total_tris + 63) / 64;
+    const uint64_t cap = (uint64_t)(a.sms > 0 ? a.sms : 1) * 4;  // 256 clipping threads per SM
+    return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+template <bool EMIT>
+int launch_setup(const GeomArgs &a, cudaStream_t s)
+{
+    const unsigned g = (a.total_tris + 127) / 128;
+    if (a.eyes) {
+        k_setup<EMIT, true><<<g, 128, 0, s>>>(a);
+        k_clip<EMIT, true><<<clip_grid(a), 64, 0, s>>>(a);
+    } else {
+        k_setup<EMIT, false><<<g, 128, 0, s>>>(a);
+        k_clip<EMIT, false><<<clip_grid(a), 64, 0, s>>>(a);
+    }
+    return 2;
+}
+
+}  // namespace
+
 int launch_setup_count(const GeomArgs &a, cudaStream_t s)
 {
     if (!a.total_tris) return 0;
-    k_setup<false><<<(a.total_tris + 127) / 128, 128, 0, s>>>(a);
-    return 1;
+    cudaMemsetAsync(a.clip_count, 0, sizeof(uint32_t), s);
+    return launch_setup<false>(a, s);
 }
 
 int launch_setup_emit(const GeomArgs &a, cudaStream_t s)
 {
     if (!a.total_tris) return 0;
-    k_setup<true><<<(a.total_tris + 127) / 128, 128, 0, s>>>(a);
-    return 1;
+    return launch_setup<true>(a, s);
 }
 
 }  // namespace mtgl

@@ -261,7 +261,7 @@ constexpr int kRadixThreads = 256;
 constexpr int kRadixWarps = kRadixThreads / 32;
 constexpr int kRadixItems = 8;  // per thread
 constexpr int kRadixTile = kRadixThreads * kRadixItems;
-constexpr int kRadixDigits = 256;
+constexpr int kRadixDigits = 512;  // up to 9-bit digits; a sort uses ceil(bits / 9) balanced passes
 
 size_t radix_hist_words(uint32_t npairs)
 {
@@ -274,8 +274,9 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t *ke
                                                              uint32_t *hist, uint32_t nblocks)
 {
     const uint32_t n = min(*n_dev, cap);
+    const int ndig = (int)mask + 1;
     __shared__ uint32_t h[kRadixDigits];
-    for (int i = threadIdx.x; i < kRadixDigits; i += kRadixThreads) h[i] = 0;
+    for (int i = threadIdx.x; i < ndig; i += kRadixThreads) h[i] = 0;
     __syncthreads();
     const uint32_t base = blockIdx.x * (uint32_t)kRadixTile;
 #pragma unroll
@@ -284,7 +285,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t *ke
         if (i < n) atomicAdd(&h[(keys[i] >> shift) & mask], 1u);
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < kRadixDigits; d += kRadixThreads) hist[(size_t)d * nblocks + blockIdx.x] = h[d];
+    for (int d = threadIdx.x; d < ndig; d += kRadixThreads) hist[(size_t)d * nblocks + blockIdx.x] = h[d];
 }
 
 // Stable scatter: warp w owns items [w*256, w*256+256) of the block, taken 32 at a time in
@@ -298,6 +299,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t 
 {
     __shared__ uint32_t wcount[kRadixWarps][kRadixDigits];
     const uint32_t n = min(*n_dev, cap);
+    const int ndig = (int)mask + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kRadixWarps * kRadixDigits; i += kRadixThreads) (&wcount[0][0])[i] = 0;
     __syncthreads();
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t 
         rank[k] = pre + __popc(peers & lt);
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < kRadixDigits; d += kRadixThreads) {
+    for (int d = threadIdx.x; d < ndig; d += kRadixThreads) {
         uint32_t run = hist_scan[(size_t)d * nblocks + blockIdx.x];
 #pragma unroll
         for (int w = 0; w < kRadixWarps; w++) {
@@ -349,12 +351,14 @@ int launch_bin_sort(BinArgs &a, cudaStream_t s)
     int launches = 0;
     int bits = 1;
     while (bits < 32 && (1u << bits) < a.ntiles) bits++;
+    const int passes = (bits + 8) / 9;
+    const int width = (bits + passes - 1) / passes;  // balanced digits of at most 9 bits
     const uint32_t nb = (n + kRadixTile - 1) / kRadixTile;
-    for (int shift = 0; shift < bits; shift += 8) {
-        const int nbits = (bits - shift) < 8 ? (bits - shift) : 8;
+    for (int shift = 0; shift < bits; shift += width) {
+        const int nbits = (bits - shift) < width ? (bits - shift) : width;
         const uint32_t mask = (1u << nbits) - 1u;
         k_radix_hist<<<nb, kRadixThreads, 0, s>>>(a.keys, n, a.total_dev, shift, mask, a.radix_hist, nb);
-        launches += 2 + launch_scan(a.radix_hist, a.radix_hist, nb * kRadixDigits, a.scan_temp, a.sort_total_dev, s);
+        launches += 2 + launch_scan(a.radix_hist, a.radix_hist, nb * (mask + 1u), a.scan_temp, a.sort_total_dev, s);
         k_radix_scatter<<<nb, kRadixThreads, 0, s>>>(a.keys, a.vals, n, a.total_dev, shift, mask, a.radix_hist, nb,
                                                      a.keys_alt, a.vals_alt);
         uint32_t *tk = a.keys, *tv = a.vals;

@@ -51,21 +51,30 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__re
                                             int py, float fpx, float fpy, uint32_t &col, float &dep, uint32_t &st,
                                             uint32_t &frags)
 {
-    if (px < __float_as_int(r[R_MINX]) || px > __float_as_int(r[R_MAXX]) || py < __float_as_int(r[R_MINY]) ||
-        py > __float_as_int(r[R_MAXY]))
+    // the record is read as 16-byte words (RecField positions noted beside each use)
+    const float4 *r4 = reinterpret_cast<const float4 *>(r);
+    const float4 q1 = __ldg(r4 + 1);  // X2 Y2 MINX MINY
+    const float4 q2 = __ldg(r4 + 2);  // MAXX MAXY AREA INV_AREA
+    if (px < __float_as_int(q1.z) || px > __float_as_int(q2.x) || py < __float_as_int(q1.w) ||
+        py > __float_as_int(q2.y))
         return false;
+    const float4 q0 = __ldg(r4 + 0);   // X0 Y0 X1 Y1
+    const float4 q12 = __ldg(r4 + 12);  // FLAGS EA0 EB0 EA1
+    const float4 q13 = __ldg(r4 + 13);  // EB1 EA2 EB2 FRAME
     // edge_function at the integer pixel position (raster.c:299-302, 534-536)
-    const float e0 = (fpx - r[R_X1]) * r[R_EA0] - (fpy - r[R_Y1]) * r[R_EB0];
-    const float e1 = (fpx - r[R_X2]) * r[R_EA1] - (fpy - r[R_Y2]) * r[R_EB1];
-    const float e2 = (fpx - r[R_X0]) * r[R_EA2] - (fpy - r[R_Y0]) * r[R_EB2];
-    const float area = r[R_AREA];
+    const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
+    const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
+    const float e2 = (fpx - q0.x) * q13.y - (fpy - q0.y) * q13.z;
+    const float area = q2.z;
     if (!((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) || (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0))) return false;
     frags++;
-    const float inv_area = r[R_INV_AREA];
+    const float inv_area = q2.w;
     const float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
-    const DevRaster &R = A.rasters[min(__float_as_uint(r[R_RASTER]), A.nrasters - 1)];
+    const float4 q3 = __ldg(r4 + 3);    // Z0 Z1 Z2 DMIN
+    const float4 q11 = __ldg(r4 + 11);  // EZ0 EZ1 EZ2 RASTER
+    const DevRaster &R = A.rasters[min(__float_as_uint(q11.w), A.nrasters - 1)];
     const mtgl_raster_state &rs = R.rs;
-    const float z = b0 * r[R_Z0] + b1 * r[R_Z1] + b2 * r[R_Z2];
+    const float z = b0 * q3.x + b1 * q3.y + b2 * q3.z;
     const float depth = map_depth(R, z);
 
     uint32_t sv = 0;
@@ -85,16 +94,16 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__re
         st = stencil_write(st, stencil_apply(rs.stencil_zpass, sv, rs.stencil_ref), rs.stencil_writemask);
 
     float4 c;
+    const float4 c2 = __ldg(r4 + 7);  // C2
     if (rs.shade_model == GL_FLAT) {
-        c = make_float4(r[R_C2], r[R_C2 + 1], r[R_C2 + 2], r[R_C2 + 3]);
+        c = c2;
     } else {
-        c = make_float4(r[R_C0] * b0 + r[R_C1] * b1 + r[R_C2] * b2,
-                        r[R_C0 + 1] * b0 + r[R_C1 + 1] * b1 + r[R_C2 + 1] * b2,
-                        r[R_C0 + 2] * b0 + r[R_C1 + 2] * b1 + r[R_C2 + 2] * b2,
-                        r[R_C0 + 3] * b0 + r[R_C1 + 3] * b1 + r[R_C2 + 3] * b2);
+        const float4 c0 = __ldg(r4 + 5), c1 = __ldg(r4 + 6);  // C0, C1
+        c = make_float4(c0.x * b0 + c1.x * b1 + c2.x * b2, c0.y * b0 + c1.y * b1 + c2.y * b2,
+                        c0.z * b0 + c1.z * b1 + c2.z * b2, c0.w * b0 + c1.w * b1 + c2.w * b2);
     }
     if (EYE && rs.lighting && have_eye) {
-        const bool back = (__float_as_uint(r[R_FLAGS]) & 1u) != 0;
+        const bool back = (__float_as_uint(q12.x) & 1u) != 0;
         const bool phong = rs.shade_model == GL_PHONG;
         if (phong || (back && rs.lit.two_side)) {
             float3 ep = make_float3(e[0] * b0 + e[6] * b1 + e[12] * b2, e[1] * b0 + e[7] * b1 + e[13] * b2,
@@ -111,18 +120,21 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__re
     }
     if (TEX && R.tex) {
         float u, v;
+        const float4 q4 = __ldg(r4 + 4);  // W0 W1 W2 LOD
         if (rs.perspective_hint != GL_FASTEST) {
-            const float uow = b0 * r[R_UW0] + b1 * r[R_UW1] + b2 * r[R_UW2];
-            const float vow = b0 * r[R_VW0] + b1 * r[R_VW1] + b2 * r[R_VW2];
-            const float oow = b0 * r[R_W0] + b1 * r[R_W1] + b2 * r[R_W2];
+            const float4 q9 = __ldg(r4 + 9), q10 = __ldg(r4 + 10);  // UV2 UW0 VW0 | UW1 VW1 UW2 VW2
+            const float uow = b0 * q9.z + b1 * q10.x + b2 * q10.z;
+            const float vow = b0 * q9.w + b1 * q10.y + b2 * q10.w;
+            const float oow = b0 * q4.x + b1 * q4.y + b2 * q4.z;
             const float w = 1.0f / oow;
             u = uow * w;
             v = vow * w;
         } else {
-            u = b0 * r[R_UV0] + b1 * r[R_UV1] + b2 * r[R_UV2];
-            v = b0 * r[R_UV0 + 1] + b1 * r[R_UV1 + 1] + b2 * r[R_UV2 + 1];
+            const float4 q8 = __ldg(r4 + 8), q9 = __ldg(r4 + 9);  // UV0 UV1 | UV2 ..
+            u = b0 * q8.x + b1 * q8.z + b2 * q9.x;
+            v = b0 * q8.y + b1 * q8.w + b2 * q9.y;
         }
-        const float4 tc = unpack_rgba(sample_lod(R, u, v, r[R_LOD]));
+        const float4 tc = unpack_rgba(sample_lod(R, u, v, q4.w));
         // the alpha test applies to textured fragments only (raster.c:639-643)
         if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) return false;
         switch (rs.tex_env_mode) {
@@ -138,7 +150,7 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__re
         }
     }
     if (rs.fog) {
-        const float fc = b0 * r[R_EZ0] + b1 * r[R_EZ1] + b2 * r[R_EZ2];
+        const float fc = b0 * q11.x + b1 * q11.y + b2 * q11.z;
         c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, fc));
     }
     bool wrote = false;

@@ -89,18 +89,6 @@ int record_after(mtgl_batch *b)
     return MTGL_OK;
 }
 
-int persistent_ctas(mtgl_batch *b, const Tables &t)
-{
-    TileArgs probe;
-    memset(&probe, 0, sizeof(probe));
-    probe.tile_shift = t.tile_shift;
-    probe.any_texture = t.any_texture ? 1 : 0;
-    probe.eye_records = t.eye ? reinterpret_cast<const float *>(1) : nullptr;
-    const int occ = tile_occupancy(probe);
-    const int per_sm = b->cfg.ctas_per_sm > 0 ? std::min(b->cfg.ctas_per_sm, occ) : occ;
-    return std::max(1, per_sm) * b->x.sms;
-}
-
 int launch_run(mtgl_batch *b)
 {
     const bool was_profiling = b->x.profile;
@@ -363,7 +351,7 @@ int mtgl_dev_batch_launch(mtgl_batch *b)
     b->run.exact = false;
     b->run.rec_cap = rec_cap;
     b->run.pair_cap = pair_cap;
-    b->run.ctas = persistent_ctas(b, b->t);
+    b->run.ctas = persistent_ctas(b->x, b->t, b->cfg.ctas_per_sm);
     b->run.order = b->cfg.order_by_cost != 0;
     if ((st = launch_run(b))) return st;
     if ((st = b->stage.mark_uploaded(b->x.stream))) return st;

@@ -147,6 +147,9 @@ struct Tables {
 int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframes, int tile_shift, bool may_grow,
                  Tables &t);
 
+// CTAs of a persistent tile launch for these tables: per_sm per SM (0: all that fit)
+int persistent_ctas(const Exec &x, const Tables &t, int per_sm);
+
 struct PipeConfig {
     bool exact = true;       // wait for the record and pair totals and size scratch from them
     uint32_t rec_cap = 0;    // capacity mode: records and tile pairs the scratch holds

@@ -60,6 +60,7 @@ struct BinArgs {
     uint32_t *keys, *vals;      // pair buffers (capacity >= pairs)
     uint32_t *keys_alt, *vals_alt;
     uint32_t *tile_count;       // per tile (ntiles + 1 entries)
+    uint32_t *tile_area;        // per tile: pixels of its records' boxes inside it, summed (may be null)
     uint32_t *tile_start;       // exclusive scan of tile_count
     uint32_t *radix_hist;       // radix histograms
     uint32_t *scan_temp;
@@ -76,12 +77,15 @@ int launch_bin_expand(const BinArgs &a, cudaStream_t s);
 int launch_bin_sort(BinArgs &a, cudaStream_t s);
 size_t radix_hist_words(uint32_t npairs);
 
-// Work order of a persistent tile launch: tile ids by descending record count (coarse
-// log buckets), so the longest tiles start first. order holds ntiles words, hist
-// kOrderHistWords.
-int launch_tile_order(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist, uint32_t *order, int sms,
-                      cudaStream_t s);
-constexpr size_t kOrderHistWords = 512;
+// Work order of the persistent tile launches. Tiles whose records are small (their boxes
+// cover on average less than a quarter of the tile) come first, then the others; each group
+// by descending record count (coarse log buckets), so the longest tiles start first. The
+// split point is written to aux[kOrderSplit]. order holds ntiles words, aux kOrderAuxWords.
+int launch_tile_order(const uint32_t *tile_count, const uint32_t *tile_area, uint32_t ntiles, int tile_shift,
+                      uint32_t *aux, uint32_t *order, int sms, cudaStream_t s);
+constexpr size_t kOrderSplit = 1024;      // aux word: number of small-record tiles
+constexpr size_t kOrderQueues = 1028;     // aux words: work-queue heads of the tile launches
+constexpr size_t kOrderAuxWords = 1040;
 
 struct TileArgs {
     const float *records;
@@ -96,7 +100,8 @@ struct TileArgs {
     uint32_t nframes;
     uint32_t ntiles;             // work items: global tile ids
     const uint32_t *order;       // item -> tile (null: item i is tile i)
-    uint32_t *queue;             // work-queue head, zero at launch
+    const uint32_t *split;       // items [0, *split) have small records (null: no split)
+    uint32_t *queue;             // work-queue heads (two), zero at launch
     int32_t ctas;                // persistent CTAs (0: one per tile)
     int32_t tile_shift;
     int32_t any_texture;         // some raster state of the pass samples a texture

@@ -313,6 +313,18 @@ int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframe
     return MTGL_OK;
 }
 
+int persistent_ctas(const Exec &x, const Tables &t, int per_sm)
+{
+    TileArgs probe;
+    memset(&probe, 0, sizeof(probe));
+    probe.tile_shift = t.tile_shift;
+    probe.any_texture = t.any_texture ? 1 : 0;
+    probe.eye_records = t.eye ? reinterpret_cast<const float *>(1) : nullptr;
+    const int occ = tile_occupancy(probe);
+    const int n = per_sm > 0 ? std::min(per_sm, occ) : occ;
+    return std::max(1, n) * x.sms;
+}
+
 // ------------------------------------------------------------------ the pipeline
 
 int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &t, const PipeConfig &c,
@@ -339,10 +351,12 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if ((rc = sc.take(S_TRI_OFFSETS, tris, &tri_offsets))) return rc;
     uint32_t *clip_list = nullptr;
     if ((rc = sc.take(S_CLIP_LIST, tris, &clip_list))) return rc;
-    if ((rc = sc.take(S_TILE_COUNT, (size_t)ntiles + 1, &tile_count))) return rc;
+    // tile counts, then (persistent ordered launches) the per-tile record-box coverage
+    if ((rc = sc.take(S_TILE_COUNT, 2 * ((size_t)ntiles + 1), &tile_count))) return rc;
+    uint32_t *tile_area = (c.ctas && c.order) ? tile_count + ntiles + 1 : nullptr;
     if ((rc = sc.take(S_TILE_START, (size_t)ntiles + 1, &tile_start))) return rc;
     if (c.ctas && c.order && (rc = sc.take(S_ORDER, ntiles, &order))) return rc;
-    if (c.ctas && (rc = sc.take(S_ORDER_AUX, kOrderHistWords + 32, &order_aux))) return rc;
+    if (c.ctas && (rc = sc.take(S_ORDER_AUX, kOrderAuxWords, &order_aux))) return rc;
     uint32_t scan_n = std::max<uint32_t>(std::max(tris, ntiles), 1);
     if (!c.exact) {
         scan_n = std::max<uint32_t>(scan_n, c.rec_cap);
@@ -408,7 +422,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     x.prof_mark();
 
     // ---- binning
-    CK(cudaMemsetAsync(tile_count, 0, ((size_t)ntiles + 1) * sizeof(uint32_t), s));
+    CK(cudaMemsetAsync(tile_count, 0, (tile_area ? 2 : 1) * ((size_t)ntiles + 1) * sizeof(uint32_t), s));
     BinArgs ba;
     memset(&ba, 0, sizeof(ba));
     ba.records = records;
@@ -420,6 +434,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ba.ntiles = ntiles;
     ba.rec_tiles = rec_tiles;
     ba.tile_count = tile_count;
+    ba.tile_area = tile_area;
     ba.tile_start = tile_start;
     ba.total_dev = x.d_totals + 1;
     ba.sort_total_dev = x.d_totals + 3;
@@ -474,11 +489,13 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ta.any_texture = t.any_texture ? 1 : 0;
     ta.fragments = x.d_frags;
     if (c.ctas) {
-        ta.queue = order_aux + kOrderHistWords;
-        CK(cudaMemsetAsync(ta.queue, 0, sizeof(uint32_t), s));
-        if (order) {
-            launches += launch_tile_order(tile_count, ntiles, order_aux, order, x.sms, s);
+        ta.queue = order_aux + kOrderQueues;
+        if (order) {  // clears the queue heads too
+            launches += launch_tile_order(tile_count, tile_area, ntiles, t.tile_shift, order_aux, order, x.sms, s);
             ta.order = order;
+            ta.split = order_aux + kOrderSplit;
+        } else {
+            CK(cudaMemsetAsync(ta.queue, 0, 2 * sizeof(uint32_t), s));
         }
         ta.ctas = c.ctas;
     }

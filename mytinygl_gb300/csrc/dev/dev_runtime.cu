@@ -124,6 +124,19 @@ int run_clears_only(mtgl_dev *d)
     return MTGL_OK;
 }
 
+// Exact sizing. A large pass runs the tile kernel persistently over the classified,
+// cost-ordered tile list (two launches); a small one, where those extra launches would cost
+// more than they save, with one CTA per tile.
+PipeConfig plain_config(mtgl_dev *d, const Tables &t)
+{
+    PipeConfig c;
+    if (t.tris >= 32768) {
+        c.ctas = persistent_ctas(d->x, t, 0);
+        c.order = true;
+    }
+    return c;
+}
+
 int flush_pass(mtgl_dev *d)
 {
     int st = mtgl_dev_enter(d);
@@ -133,7 +146,7 @@ int flush_pass(mtgl_dev *d)
     FrameSrc fs{d, &P, 0};
     Tables t;
     if ((st = build_tables(d->x, d->stage, &fs, 1, kTileShiftPlain, true, t))) return st;
-    PipeConfig c;  // exact sizing, one CTA per tile
+    PipeConfig c = plain_config(d, t);
     PipeOut o;
     if ((st = run_pipeline(d->x, d->x.pool, d->stage, t, c, &o))) return st;
     if ((st = d->stage.mark_uploaded(d->x.stream))) return st;
@@ -664,7 +677,7 @@ int flush_pass_noalloc(mtgl_dev *d)
                      "mtgl_flush_noalloc: the pass's tables exceed the context's staging areas; the pass stays queued");
         return st;
     }
-    PipeConfig c;
+    PipeConfig c = plain_config(d, t);
     PipeOut o;
     if ((st = run_pipeline(d->x, cv, d->stage, t, c, &o))) {
         d->stage.used = used0;  // drop the tables; the pass stays queued

@@ -156,6 +156,10 @@ __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
     for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
         int tx0, ty0, tx1, ty1;
         const DevFrame &F = rec_tile_box(A.records + (size_t)r * kRecWords, A, tx0, ty0, tx1, ty1);
+        const float4 b1 = __ldg(reinterpret_cast<const float4 *>(A.records + (size_t)r * kRecWords) + 1);
+        const float4 b2 = __ldg(reinterpret_cast<const float4 *>(A.records + (size_t)r * kRecWords) + 2);
+        const int bx0 = __float_as_int(b1.z), by0 = __float_as_int(b1.w);
+        const int bx1 = __float_as_int(b2.x), by1 = __float_as_int(b2.y);
         const int w = tx1 - tx0 + 1;
         const int cnt = w * (ty1 - ty0 + 1);
         const uint32_t base = A.rec_tiles[r];
@@ -166,6 +170,12 @@ __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
             A.keys[base + i] = tile;
             A.vals[base + i] = r;
             atomicAdd(A.tile_count + tile, 1u);
+            if (A.tile_area) {  // pixels of the record's box inside this tile
+                const int sh = A.tile_shift;
+                const int ox = min(bx1, ((tx + 1) << sh) - 1) - max(bx0, tx << sh) + 1;
+                const int oy = min(by1, ((ty + 1) << sh) - 1) - max(by0, ty << sh) + 1;
+                atomicAdd(A.tile_area + tile, (uint32_t)(ox * oy));
+            }
         }
     }
 }
@@ -203,30 +213,46 @@ __device__ __forceinline__ uint32_t cost_bucket(uint32_t c)
     return min(1u + (uint32_t)lg * 8u + frac, 255u);
 }
 
-// hist[0..255]: tiles per bucket; hist[256..511]: placement cursors (both zero at launch)
-__global__ void __launch_bounds__(256) k_order_hist(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist)
+// A tile's class: 0 when its records are small (their boxes cover on average under a quarter
+// of the tile), else 1. Empty tiles are class 1.
+__device__ __forceinline__ uint32_t tile_class(const uint32_t *tile_count, const uint32_t *tile_area, uint32_t t,
+                                               int tile_shift)
 {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
-        atomicAdd(&h[cost_bucket(tile_count[t])], 1u);
-    __syncthreads();
-    if (h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+    const uint32_t c = tile_count[t];
+    if (c == 0 || !tile_area) return 1u;
+    return (uint64_t)tile_area[t] * 4u < ((uint64_t)c << (2 * tile_shift)) ? 0u : 1u;
 }
 
-// Places every tile after all tiles of costlier buckets. The order inside a bucket is
-// whatever the atomics give: tiles are independent, so the order changes timing only.
-__global__ void __launch_bounds__(256) k_order_scatter(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist,
+// aux[0..511]: tiles per (class, bucket); aux[512..1023]: placement cursors; all zero at launch
+__global__ void __launch_bounds__(256) k_order_hist(const uint32_t *tile_count, const uint32_t *tile_area,
+                                                    uint32_t ntiles, int tile_shift, uint32_t *aux)
+{
+    __shared__ uint32_t h[512];
+    h[threadIdx.x] = 0;
+    h[threadIdx.x + 256] = 0;
+    __syncthreads();
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+        atomicAdd(&h[tile_class(tile_count, tile_area, t, tile_shift) * 256 + cost_bucket(tile_count[t])], 1u);
+    __syncthreads();
+    if (h[threadIdx.x]) atomicAdd(&aux[threadIdx.x], h[threadIdx.x]);
+    if (h[threadIdx.x + 256]) atomicAdd(&aux[threadIdx.x + 256], h[threadIdx.x + 256]);
+}
+
+// Places every tile after all tiles of earlier groups: class 0 before class 1, costlier
+// buckets first within a class. The order inside a bucket is whatever the atomics give:
+// tiles are independent, so it changes timing only.
+__global__ void __launch_bounds__(256) k_order_scatter(const uint32_t *tile_count, const uint32_t *tile_area,
+                                                       uint32_t ntiles, int tile_shift, uint32_t *aux,
                                                        uint32_t *order)
 {
-    __shared__ uint32_t start[256];
+    __shared__ uint32_t start[512];
     __shared__ uint32_t warp_tot[8];
-    // exclusive prefix over buckets in descending order: bucket b starts after buckets > b
-    const int b = 255 - (int)threadIdx.x;
-    const uint32_t v = hist[b];
+    // positions p = 2*thread, 2*thread+1 in placement order: class p / 256, bucket 255 - p % 256
+    const int p0 = 2 * (int)threadIdx.x, p1 = p0 + 1;
+    const int e0 = (p0 / 256) * 256 + (255 - p0 % 256), e1 = (p1 / 256) * 256 + (255 - p1 % 256);
+    const uint32_t v0 = aux[e0], v1 = aux[e1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
+    uint32_t x = v0 + v1;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -236,22 +262,25 @@ __global__ void __launch_bounds__(256) k_order_scatter(const uint32_t *tile_coun
     __syncthreads();
     uint32_t before = 0;
     for (int w = 0; w < warp; w++) before += warp_tot[w];
-    start[b] = before + x - v;
+    const uint32_t excl = before + x - (v0 + v1);
+    start[e0] = excl;
+    start[e1] = excl + v0;
+    if (blockIdx.x == 0 && threadIdx.x == 127) aux[kOrderSplit] = before + x;  // end of class 0
     __syncthreads();
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
-        const uint32_t bk = cost_bucket(tile_count[t]);
-        order[start[bk] + atomicAdd(&hist[256 + bk], 1u)] = t;
+        const uint32_t e = tile_class(tile_count, tile_area, t, tile_shift) * 256 + cost_bucket(tile_count[t]);
+        order[start[e] + atomicAdd(&aux[512 + e], 1u)] = t;
     }
 }
 
-int launch_tile_order(const uint32_t *tile_count, uint32_t ntiles, uint32_t *hist, uint32_t *order, int sms,
-                      cudaStream_t s)
+int launch_tile_order(const uint32_t *tile_count, const uint32_t *tile_area, uint32_t ntiles, int tile_shift,
+                      uint32_t *aux, uint32_t *order, int sms, cudaStream_t s)
 {
     if (!ntiles) return 0;
-    cudaMemsetAsync(hist, 0, kOrderHistWords * sizeof(uint32_t), s);
+    cudaMemsetAsync(aux, 0, kOrderAuxWords * sizeof(uint32_t), s);
     const unsigned g = stride_grid(ntiles, 256, sms);
-    k_order_hist<<<g, 256, 0, s>>>(tile_count, ntiles, hist);
-    k_order_scatter<<<g, 256, 0, s>>>(tile_count, ntiles, hist, order);
+    k_order_hist<<<g, 256, 0, s>>>(tile_count, tile_area, ntiles, tile_shift, aux);
+    k_order_scatter<<<g, 256, 0, s>>>(tile_count, tile_area, ntiles, tile_shift, aux, order);
     return 2;
 }
 

@@ -248,6 +248,24 @@ __device__ __noinline__ PixelOut shade_prim(const TileArgs &A, const float *r, i
     return point_ops(rs, depth, c, col, dep);
 }
 
+// One covered fragment of record `ridx` for this thread's pixel, whatever the record draws.
+template <bool TEX, bool EYE>
+__device__ __forceinline__ bool shade_any(const TileArgs &A, uint32_t ridx, uint32_t rflags, bool have_eye, int px,
+                                          int py, float fpx, float fpy, uint32_t &col, float &dep, uint32_t &st,
+                                          uint32_t &frags)
+{
+    const float *r = A.records + (size_t)ridx * kRecWords;
+    if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {
+        const float *e = have_eye ? A.eye_records + (size_t)ridx * kEyeWords : nullptr;
+        return shade_pixel<TEX, EYE>(A, r, e, have_eye, px, py, fpx, fpy, col, dep, st, frags);
+    }
+    const PixelOut po = shade_prim(A, r, px, py, col, dep);
+    col = po.col;
+    dep = po.dep;
+    frags += po.flags & 1u;
+    return (po.flags & 2u) != 0;
+}
+
 // Without per-fragment lighting the kernel fits 48 registers: ask for 1280 resident
 // threads per SM (5 CTAs of 16x16, 20 of 8x8); with it, 64 registers and 1024 threads. A
 // 32x32 CTA is 1024 threads on its own.
@@ -257,7 +275,16 @@ constexpr int tile_min_blocks()
     return TS == 32 ? 1 : (EYE ? 1024 : 1280) / (TS * TS);
 }
 
-template <int TS, bool TEX, bool EYE>
+// ROUNDS selects how a warp runs the fragments of its records, both in submission order per
+// pixel (the tile order puts tiles of small records in the first part of the work list):
+// - per record (ROUNDS false): the warp steps through the records meeting its 8x4 block,
+//   each covered lane runs the fragment pipeline, and the depth rejection is retried with
+//   the warp's max depth as it falls;
+// - by rounds (ROUNDS true, small records): every lane first finds the records covering
+//   its pixel (broadcast reads), then takes its next covering record per round, so the
+//   fragment pipeline runs with most lanes busy; rounds = the deepest coverage among the
+//   warp's pixels, instead of the number of records meeting the block.
+template <int TS, bool TEX, bool EYE, bool ROUNDS>
 __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(TileArgs A)
 {
     constexpr int kThreads = TS * TS;
@@ -273,12 +300,20 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
 
     for (uint32_t item = blockIdx.x;;) {
         if (A.ctas) {
-            if (threadIdx.x == 0) s_tile = atomicAdd(A.queue, 1u);
+            if (threadIdx.x == 0) {
+                // this launch's items: the small-record part of the list, or the rest
+                const uint32_t split = A.split ? min(*A.split, A.ntiles) : 0u;
+                const uint32_t lo = ROUNDS ? 0u : split, hi = ROUNDS ? split : A.ntiles;
+                const uint32_t it = lo + atomicAdd(A.queue + (ROUNDS ? 0 : 1), 1u);
+                s_tile = it < hi ? it : 0xFFFFFFFFu;
+            }
             __syncthreads();
             item = s_tile;
             __syncthreads();
+            if (item == 0xFFFFFFFFu) break;
+        } else if (item >= A.ntiles) {
+            break;
         }
-        if (item >= A.ntiles) break;
         const uint32_t tile = A.order ? A.order[item] : item;
         if (!A.ctas) item = A.ntiles;  // one tile per CTA
         // the frame owning the tile: last frame whose tile_base <= tile
@@ -371,30 +406,54 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                     take = false;
             }
             uint32_t todo = __ballot_sync(0xffffffffu, take);
-            while (todo) {
-                const int j = __ffs(todo) - 1;
-                todo &= todo - 1;
-                const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
-                const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                const float rdmin = __shfl_sync(0xffffffffu, dmin, j);
-                // warp-uniform rejection: no fragment of this triangle can pass the depth test here
-                const uint32_t zc = (rflags >> 1) & 3u;
-                if (zc != ZC_NONE) {
-                    if (zc == ZC_NEVER || rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax)) continue;
+            if (ROUNDS) {
+                uint32_t cov = 0;
+                while (todo) {
+                    const int j = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                    const float4 *q = recs4 + (size_t)ridx * (kRecWords / 4);
+                    const float4 q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+                    bool in = !(px < __float_as_int(q1.z) || px > __float_as_int(q2.x) ||
+                                py < __float_as_int(q1.w) || py > __float_as_int(q2.y));
+                    if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {  // points and lines test when shaded
+                        const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
+                        const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
+                        const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
+                        const float e2 = (fpx - q0.x) * q13.y - (fpy - q0.y) * q13.z;
+                        const float area = q2.z;
+                        in = in && ((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) ||
+                                    (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0));
+                    }
+                    if (in) cov |= 1u << j;
                 }
-                const float *r = A.records + (size_t)ridx * kRecWords;
-                bool wrote;
-                if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {
-                    const float *e = have_eye ? A.eye_records + (size_t)ridx * kEyeWords : nullptr;
-                    wrote = shade_pixel<TEX, EYE>(A, r, e, have_eye, px, py, fpx, fpy, col, dep, st, frags);
-                } else {
-                    const PixelOut po = shade_prim(A, r, px, py, col, dep);
-                    col = po.col;
-                    dep = po.dep;
-                    frags += po.flags & 1u;
-                    wrote = (po.flags & 2u) != 0;
+                while (__any_sync(0xffffffffu, cov != 0)) {
+                    const int j = cov ? __ffs(cov) - 1 : 0;
+                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                    bool wrote = false;
+                    if (cov) {
+                        cov &= cov - 1;
+                        wrote = shade_any<TEX, EYE>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags);
+                    }
+                    if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
                 }
-                if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
+            } else {
+                while (todo) {
+                    const int j = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                    const float rdmin = __shfl_sync(0xffffffffu, dmin, j);
+                    // warp-uniform rejection: no fragment of this triangle can pass the depth test here
+                    const uint32_t zc = (rflags >> 1) & 3u;
+                    if (zc == ZC_NEVER || (zc != ZC_NONE && (rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax))))
+                        continue;
+                    const bool wrote =
+                        shade_any<TEX, EYE>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags);
+                    if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
+                }
             }
         }
 
@@ -417,16 +476,23 @@ struct TileVariant {
         static int occ = -1;
         if (occ < 0) {
             int n = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tile<TS, TEX, EYE>, TS * TS, 0) != cudaSuccess)
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tile<TS, TEX, EYE, false>, TS * TS, 0) !=
+                cudaSuccess)
                 n = 1;
             occ = n > 0 ? n : 1;
         }
         return occ;
     }
-    static void launch(const TileArgs &a, cudaStream_t s)
+    static int launch(const TileArgs &a, cudaStream_t s)
     {
         const unsigned grid = a.ctas ? (unsigned)std::min<uint32_t>((uint32_t)a.ctas, a.ntiles) : a.ntiles;
-        k_tile<TS, TEX, EYE><<<grid, TS * TS, 0, s>>>(a);
+        if (a.split && a.ctas) {  // small-record tiles by rounds, then the rest per record
+            k_tile<TS, TEX, EYE, true><<<grid, TS * TS, 0, s>>>(a);
+            k_tile<TS, TEX, EYE, false><<<grid, TS * TS, 0, s>>>(a);
+            return 2;
+        }
+        k_tile<TS, TEX, EYE, false><<<grid, TS * TS, 0, s>>>(a);
+        return 1;
     }
 };
 
@@ -434,10 +500,12 @@ template <int TS>
 int dispatch_tile(const TileArgs &a, cudaStream_t s, bool occ_only)
 {
     const bool eye = a.eye_records != nullptr;
-    if (a.any_texture && eye) return occ_only ? TileVariant<TS, true, true>::occupancy() : (TileVariant<TS, true, true>::launch(a, s), 1);
-    if (a.any_texture) return occ_only ? TileVariant<TS, true, false>::occupancy() : (TileVariant<TS, true, false>::launch(a, s), 1);
-    if (eye) return occ_only ? TileVariant<TS, false, true>::occupancy() : (TileVariant<TS, false, true>::launch(a, s), 1);
-    return occ_only ? TileVariant<TS, false, false>::occupancy() : (TileVariant<TS, false, false>::launch(a, s), 1);
+    if (a.any_texture && eye)
+        return occ_only ? TileVariant<TS, true, true>::occupancy() : TileVariant<TS, true, true>::launch(a, s);
+    if (a.any_texture)
+        return occ_only ? TileVariant<TS, true, false>::occupancy() : TileVariant<TS, true, false>::launch(a, s);
+    if (eye) return occ_only ? TileVariant<TS, false, true>::occupancy() : TileVariant<TS, false, true>::launch(a, s);
+    return occ_only ? TileVariant<TS, false, false>::occupancy() : TileVariant<TS, false, false>::launch(a, s);
 }
 
 int dispatch_tile_size(const TileArgs &a, cudaStream_t s, bool occ_only)

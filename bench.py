@@ -520,7 +520,8 @@ def run_batch(args, spec):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded; mytinygl_gb300/workloads.py uneven_batch)",
-        "config": {"workload": spec["name"], "description": spec["desc"], "frames_per_step": BATCH_FRAMES,
+        "config": {"workload": spec["name"] if BATCH_FRAMES == 256 else f"uneven_batch_{BATCH_FRAMES}_frames",
+                   "description": spec["desc"], "frames_per_step": BATCH_FRAMES,
                    "pixels_per_step": npix, "input_triangles_per_step": tris,
                    "setup_triangles_per_step": int(rec), "bin_entries_per_step": int(pairs),
                    "tile": bst["tile_size"], "persistent_ctas": bst["ctas"],

@@ -155,7 +155,8 @@ struct PipeConfig {
     uint32_t rec_cap = 0;    // capacity mode: records and tile pairs the scratch holds
     uint32_t pair_cap = 0;
     int32_t ctas = 0;        // persistent tile CTAs (0: one CTA per tile)
-    bool order = false;      // hand out tiles costliest first
+    bool order = false;      // hand out tiles costliest first (classified: small-record tiles first)
+    bool classify = false;   // without an order: small-record tiles by rounds, the rest per record
 };
 
 struct PipeOut {

@@ -87,6 +87,16 @@ constexpr size_t kOrderSplit = 1024;      // aux word: number of small-record ti
 constexpr size_t kOrderQueues = 1028;     // aux words: work-queue heads of the tile launches
 constexpr size_t kOrderAuxWords = 1040;
 
+// A tile's class: 0 when its records are small (their boxes cover on average under a quarter
+// of the tile), else 1. Empty tiles are class 1.
+__device__ __forceinline__ uint32_t tile_class(const uint32_t *tile_count, const uint32_t *tile_area, uint32_t t,
+                                               int tile_shift)
+{
+    const uint32_t c = tile_count[t];
+    if (c == 0 || !tile_area) return 1u;
+    return (uint64_t)tile_area[t] * 4u < ((uint64_t)c << (2 * tile_shift)) ? 0u : 1u;
+}
+
 struct TileArgs {
     const float *records;
     const float *eye_records;
@@ -101,6 +111,8 @@ struct TileArgs {
     uint32_t ntiles;             // work items: global tile ids
     const uint32_t *order;       // item -> tile (null: item i is tile i)
     const uint32_t *split;       // items [0, *split) have small records (null: no split)
+    const uint32_t *tile_area;   // without an order: per-tile record-box coverage; each launch
+                                 // takes the tiles of its class in tile order (null: no classes)
     uint32_t *queue;             // work-queue heads (two), zero at launch
     int32_t ctas;                // persistent CTAs (0: one per tile)
     int32_t tile_shift;

@@ -353,7 +353,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if ((rc = sc.take(S_CLIP_LIST, tris, &clip_list))) return rc;
     // tile counts, then (persistent ordered launches) the per-tile record-box coverage
     if ((rc = sc.take(S_TILE_COUNT, 2 * ((size_t)ntiles + 1), &tile_count))) return rc;
-    uint32_t *tile_area = (c.ctas && c.order) ? tile_count + ntiles + 1 : nullptr;
+    uint32_t *tile_area = (c.ctas && (c.order || c.classify)) ? tile_count + ntiles + 1 : nullptr;
     if ((rc = sc.take(S_TILE_START, (size_t)ntiles + 1, &tile_start))) return rc;
     if (c.ctas && c.order && (rc = sc.take(S_ORDER, ntiles, &order))) return rc;
     if (c.ctas && (rc = sc.take(S_ORDER_AUX, kOrderAuxWords, &order_aux))) return rc;
@@ -496,6 +496,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
             ta.split = order_aux + kOrderSplit;
         } else {
             CK(cudaMemsetAsync(ta.queue, 0, 2 * sizeof(uint32_t), s));
+            ta.tile_area = tile_area;  // classes, tile order
         }
         ta.ctas = c.ctas;
     }

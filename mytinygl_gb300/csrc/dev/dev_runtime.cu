@@ -124,15 +124,15 @@ int run_clears_only(mtgl_dev *d)
     return MTGL_OK;
 }
 
-// Exact sizing. A large pass runs the tile kernel persistently over the classified,
-// cost-ordered tile list (two launches); a small one, where those extra launches would cost
-// more than they save, with one CTA per tile.
+// Exact sizing. A large pass runs the tile kernel persistently in two launches, tiles of
+// small records by rounds and the rest per record, each in tile order; a small one, where
+// those extra launches would cost more than they save, with one CTA per tile.
 PipeConfig plain_config(mtgl_dev *d, const Tables &t)
 {
     PipeConfig c;
     if (t.tris >= 32768) {
         c.ctas = persistent_ctas(d->x, t, 0);
-        c.order = true;
+        c.classify = true;  // one frame: tile order keeps neighbouring tiles' records in cache together
     }
     return c;
 }

@@ -213,16 +213,6 @@ __device__ __forceinline__ uint32_t cost_bucket(uint32_t c)
     return min(1u + (uint32_t)lg * 8u + frac, 255u);
 }
 
-// A tile's class: 0 when its records are small (their boxes cover on average under a quarter
-// of the tile), else 1. Empty tiles are class 1.
-__device__ __forceinline__ uint32_t tile_class(const uint32_t *tile_count, const uint32_t *tile_area, uint32_t t,
-                                               int tile_shift)
-{
-    const uint32_t c = tile_count[t];
-    if (c == 0 || !tile_area) return 1u;
-    return (uint64_t)tile_area[t] * 4u < ((uint64_t)c << (2 * tile_shift)) ? 0u : 1u;
-}
-
 // aux[0..511]: tiles per (class, bucket); aux[512..1023]: placement cursors; all zero at launch
 __global__ void __launch_bounds__(256) k_order_hist(const uint32_t *tile_count, const uint32_t *tile_area,
                                                     uint32_t ntiles, int tile_shift, uint32_t *aux)

@@ -916,7 +916,7 @@ namespace {
 unsigned clip_grid(const GeomArgs &a)
 {
     const uint64_t want = ((uint64_t)a.total_tris + 63) / 64;
-    const uint64_t cap = (uint64_t)(a.sms > 0 ? a.sms : 1) * 4;  // 256 clipping threads per SM
+    const uint64_t cap = (uint64_t)(a.sms > 0 ? a.sms : 1) * 8;  // 512 clipping threads per SM
     return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
 }
 

@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
         if (A.ctas) {
             if (threadIdx.x == 0) {
                 // this launch's items: the small-record part of the list, or the rest
-                const uint32_t split = A.split ? min(*A.split, A.ntiles) : 0u;
+                const uint32_t split = A.split ? min(*A.split, A.ntiles) : (ROUNDS ? A.ntiles : 0u);
                 const uint32_t lo = ROUNDS ? 0u : split, hi = ROUNDS ? split : A.ntiles;
                 const uint32_t it = lo + atomicAdd(A.queue + (ROUNDS ? 0 : 1), 1u);
                 s_tile = it < hi ? it : 0xFFFFFFFFu;
@@ -316,6 +316,8 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
         }
         const uint32_t tile = A.order ? A.order[item] : item;
         if (!A.ctas) item = A.ntiles;  // one tile per CTA
+        // unordered classified launches: each takes the tiles of its own class, in tile order
+        if (A.tile_area && tile_class(A.tile_count, A.tile_area, tile, A.tile_shift) != (ROUNDS ? 0u : 1u)) continue;
         // the frame owning the tile: last frame whose tile_base <= tile
         uint32_t f = 0;
         if (A.nframes > 1) {
@@ -486,7 +488,7 @@ struct TileVariant {
     static int launch(const TileArgs &a, cudaStream_t s)
     {
         const unsigned grid = a.ctas ? (unsigned)std::min<uint32_t>((uint32_t)a.ctas, a.ntiles) : a.ntiles;
-        if (a.split && a.ctas) {  // small-record tiles by rounds, then the rest per record
+        if ((a.split || a.tile_area) && a.ctas) {  // small-record tiles by rounds, then the rest per record
             k_tile<TS, TEX, EYE, true><<<grid, TS * TS, 0, s>>>(a);
             k_tile<TS, TEX, EYE, false><<<grid, TS * TS, 0, s>>>(a);
             return 2;

@@ -398,6 +398,7 @@ int mtgl_dev_draw(mtgl_dev *d, const mtgl_draw *dr)
         if (st) return st;
         if (ntri > 0x7FFFFFFFull) return MTGL_ERR_INVALID;
     }
+    const size_t staged0 = d->stage.used;
     int st = d->stage.wait();
     if (st) return st;
 
@@ -461,6 +462,7 @@ int mtgl_dev_draw(mtgl_dev *d, const mtgl_draw *dr)
     P.slots += D.vslot_count;
     P.tris += ntri;
     P.draws.push_back(p);
+    d->stats.staged_bytes += d->stage.used - staged0;
     return MTGL_OK;
 }
 

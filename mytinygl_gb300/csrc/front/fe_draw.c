@@ -125,6 +125,66 @@ void fe_flush_immediate(GLState *c)
     c->vs_dirty = 1;
 }
 
+static void buffer_attrib(mtgl_attrib *a, mtgl_handle vb, uint64_t offset, uint64_t buffer_bytes, int size)
+{
+    memset(a, 0, sizeof(*a));
+    a->buffer = vb;
+    a->offset = offset;
+    a->bytes = buffer_bytes - offset;
+    a->size = size;
+    a->type = GL_FLOAT;
+    a->stride = (int32_t)sizeof(fe_vertex);
+    a->enabled = 1;
+}
+
+/* glCallList of a device-resident block (fe_lists.c): what glBegin, the block's commands
+ * and glEnd do through the immediate path, with the vertices read from the list's device
+ * buffer. The packet glEnd would submit has one vertex state (the block changes no state
+ * that the snapshot holds, and the snapshot is taken, as at the first emit_vertex, before
+ * GL_COLOR_MATERIAL rewrites the material); an attribute the block never sets comes from
+ * the current value, which every vertex would have copied. Afterwards the current
+ * attributes hold the block's last values, and GL_COLOR_MATERIAL under lighting leaves the
+ * last vertex's colour in the material (emit_vertex, gl_api.c:263-348). Returns 0, having
+ * done nothing, when the replay must go through the public entry points instead (a list
+ * being compiled, a glBegin still open, vertices emitted outside glBegin/glEnd pending). */
+int fe_draw_list_block(GLState *c, mtgl_handle vb, const fe_list_block *b)
+{
+    if ((c->flags & F_INSIDE_BEGIN_END) || c->list_index != 0 || c->imm_count != 0) return 0;
+    if (b->set & CL_COLOR) memcpy(c->cur_color, b->color, sizeof(c->cur_color));
+    if (b->set & CL_TEXCOORD) memcpy(c->cur_tex, b->tex, sizeof(c->cur_tex));
+    if (b->set & CL_NORMAL) memcpy(c->cur_normal, b->normal, sizeof(c->cur_normal));
+    c->prim_mode = b->mode;
+
+    const uint64_t base = (uint64_t)b->first * sizeof(fe_vertex);
+    const uint64_t bytes = base + (uint64_t)b->count * sizeof(fe_vertex);
+    mtgl_draw d;
+    memset(&d, 0, sizeof(d));
+    d.mode = b->mode;
+    d.count = (int32_t)b->count;
+    d.index_max = (int64_t)b->count - 1;
+    buffer_attrib(&d.position, vb, base + offsetof(fe_vertex, pos), bytes, 3);
+    if (b->set & CL_COLOR) buffer_attrib(&d.color, vb, base + offsetof(fe_vertex, color), bytes, 4);
+    if (b->set & CL_TEXCOORD) buffer_attrib(&d.texcoord, vb, base + offsetof(fe_vertex, tex), bytes, 2);
+    if (b->set & CL_NORMAL) buffer_attrib(&d.normal, vb, base + offsetof(fe_vertex, normal), bytes, 3);
+    memcpy(d.current_color, c->cur_color, sizeof(d.current_color));
+    memcpy(d.current_texcoord, c->cur_tex, sizeof(d.current_texcoord));
+    memcpy(d.current_normal, c->cur_normal, sizeof(d.current_normal));
+    mtgl_vertex_state vs;
+    mtgl_raster_state rs;
+    fe_snapshot_vertex(c, &vs);
+    fe_snapshot_raster(c, &rs);
+    d.vertex_states = &vs;
+    d.vertex_state_count = 1;
+    d.raster_state = &rs;
+    fe_dev_error(c, mtgl_dev_draw(c->dev, &d));
+    if ((c->flags & F_LIGHTING) && (c->flags & F_COLOR_MATERIAL))
+        apply_color_material(c, (b->set & CL_COLOR) ? b->last_color : c->cur_color);
+    c->imm_count = 0;
+    c->vs_count = 0;
+    c->vs_dirty = 1;
+    return 1;
+}
+
 void glBegin(GLenum mode)
 {
     CHECK_CTX();

@@ -108,11 +108,27 @@ typedef struct {
     double d[6];
 } fe_list_cmd;
 
+/* A glBegin/glEnd block of a display list whose vertices live in the list's device buffer.
+ * Its commands are glVertex / glColor / glTexCoord / glNormal only, and each attribute is
+ * either never set inside the block (every vertex takes the current value at call time) or
+ * set before the block's first vertex (every vertex takes values recorded in the list). */
+typedef struct {
+    size_t begin, end;           /* indices of its LC_BEGIN and LC_END commands */
+    GLenum mode;
+    uint32_t first, count;       /* its vertices in the device buffer */
+    uint32_t set;                /* CL_COLOR / CL_TEXCOORD / CL_NORMAL set inside the block */
+    float color[4], tex[2], normal[3];  /* values current after the block (when set) */
+    float last_color[4];         /* colour of the block's last vertex (when CL_COLOR is set) */
+} fe_list_block;
+
 typedef struct {
     int allocated;
     int valid;
     fe_list_cmd *cmds;
     size_t count, cap;
+    mtgl_handle vb;              /* device copy of the blocks' vertices (fe_vertex layout) */
+    fe_list_block *blocks;       /* in command order */
+    size_t nblocks;
 } fe_list;
 
 struct GLState {
@@ -265,6 +281,7 @@ static inline uint32_t fe_color_to_rgba32(const float *c)
 
 /* front-end internals shared between translation units */
 void fe_flush_immediate(GLState *c);          /* glEnd body: submit the batch */
+int fe_draw_list_block(GLState *c, mtgl_handle vb, const fe_list_block *b); /* 0: replay instead */
 void fe_snapshot_raster(GLState *c, mtgl_raster_state *rs);
 void fe_snapshot_vertex(GLState *c, mtgl_vertex_state *vs);
 fe_texture *fe_texture_get(GLState *c, GLuint id);

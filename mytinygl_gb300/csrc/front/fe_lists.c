@@ -6,6 +6,12 @@
  * GL_COMPILE); replay re-issues the public entry points, so replayed geometry reaches the
  * device through the same immediate-mode path. Ids are allocated as contiguous ranges,
  * first-fit over freed slots, capped at 1024; nested glCallList stops at depth 64.
+ *
+ * Device-resident blocks: at glEndList the vertices of every glBegin/glEnd block whose
+ * attributes do not depend on where in the block the caller's current values would show
+ * (fe_list_block) are uploaded once into one device buffer per list, and glCallList draws
+ * such a block from there (fe_draw_list_block) instead of re-emitting its vertices, which
+ * would stage them from host memory again on every call. Everything else replays.
  */
 #include "fe_internal.h"
 
@@ -16,9 +22,27 @@ fe_list *fe_list_get(GLState *c, GLuint id)
     return l->allocated ? l : NULL;
 }
 
+/* drops the device-resident blocks of a list */
+static void drop_blocks(GLState *c, fe_list *l)
+{
+    if (l->vb) (void)mtgl_dev_buffer_destroy(c->dev, l->vb);
+    free(l->blocks);
+    l->vb = 0;
+    l->blocks = NULL;
+    l->nblocks = 0;
+}
+
+/* a list slot back to its never-allocated state */
+static void clear_list(GLState *c, fe_list *l)
+{
+    drop_blocks(c, l);
+    free(l->cmds);
+    memset(l, 0, sizeof(*l));
+}
+
 void fe_lists_free(GLState *c)
 {
-    for (size_t i = 0; i < c->list_count; i++) free(c->lists[i].cmds);
+    for (size_t i = 0; i < c->list_count; i++) clear_list(c, &c->lists[i]);
     free(c->lists);
     c->lists = NULL;
     c->list_count = c->list_cap = 0;
@@ -75,6 +99,113 @@ int fe_rec_f3(fe_list_op op, float x, float y, float z)
     return fe_rec(&cmd);
 }
 
+/* Scans the block opened by the LC_BEGIN at `b`. Returns its vertex count, or 0 when it
+ * cannot be device-resident: another command before LC_END, no LC_END, an invalid mode, no
+ * vertex, or an attribute set after a vertex that took the caller's current value. With
+ * `out`, writes the vertices (fe_vertex layout; attributes the block never sets are left
+ * zero, the draw takes them from the current values; a block that turns out not to
+ * qualify may have written some). Colours are stored as recorded:
+ * LC_COLOR holds glColor's sanitised values, which replaying through glColor4f keeps. */
+static uint32_t scan_block(const fe_list *l, size_t b, fe_list_block *blk, fe_vertex *out)
+{
+    const fe_list_cmd *cmd = l->cmds;
+    const uint32_t attribs = CL_COLOR | CL_TEXCOORD | CL_NORMAL;
+    uint32_t set = 0, inherited = 0, n = 0;
+    fe_vertex cur;
+    memset(&cur, 0, sizeof(cur));
+    memset(blk, 0, sizeof(*blk));
+    if (cmd[b].e[0] > GL_POLYGON) return 0;
+    for (size_t i = b + 1; i < l->count; i++) {
+        const fe_list_cmd *m = &cmd[i];
+        switch (m->op) {
+        case LC_VERTEX:
+            if (n == UINT32_MAX / 2) return 0;
+            inherited |= attribs & ~set;
+            memcpy(cur.pos, m->f, sizeof(cur.pos));
+            if (out) out[n] = cur;
+            if (set & CL_COLOR) memcpy(blk->last_color, cur.color, sizeof(blk->last_color));
+            n++;
+            break;
+        case LC_COLOR:
+            if (inherited & CL_COLOR) return 0;
+            set |= CL_COLOR;
+            memcpy(cur.color, m->f, sizeof(cur.color));
+            break;
+        case LC_TEXCOORD:
+            if (inherited & CL_TEXCOORD) return 0;
+            set |= CL_TEXCOORD;
+            memcpy(cur.tex, m->f, sizeof(cur.tex));
+            break;
+        case LC_NORMAL:
+            if (inherited & CL_NORMAL) return 0;
+            set |= CL_NORMAL;
+            memcpy(cur.normal, m->f, sizeof(cur.normal));
+            break;
+        case LC_END:
+            if (n == 0) return 0;
+            blk->begin = b;
+            blk->end = i;
+            blk->mode = cmd[b].e[0];
+            blk->count = n;
+            blk->set = set;
+            memcpy(blk->color, cur.color, sizeof(blk->color));
+            memcpy(blk->tex, cur.tex, sizeof(blk->tex));
+            memcpy(blk->normal, cur.normal, sizeof(blk->normal));
+            return n;
+        default:
+            return 0;
+        }
+    }
+    return 0;
+}
+
+/* glEndList: uploads the list's device-resident blocks (nothing on failure: they replay) */
+static void build_blocks(GLState *c, fe_list *l)
+{
+    size_t nblocks = 0;
+    uint64_t nverts = 0;
+    fe_list_block blk;
+    for (size_t i = 0; i < l->count; i++) {
+        if (l->cmds[i].op != LC_BEGIN) continue;
+        uint32_t n = scan_block(l, i, &blk, NULL);
+        if (!n) continue;
+        nblocks++;
+        nverts += n;
+        i = blk.end;
+    }
+    if (nblocks == 0 || nverts > (uint64_t)INT32_MAX) return;
+    fe_list_block *blocks = (fe_list_block *)malloc(nblocks * sizeof(fe_list_block));
+    fe_vertex *verts = (fe_vertex *)malloc((size_t)nverts * sizeof(fe_vertex));
+    mtgl_handle vb = 0;
+    if (blocks && verts) {
+        size_t nb = 0;
+        uint32_t first = 0;
+        for (size_t i = 0; i < l->count; i++) {
+            if (l->cmds[i].op != LC_BEGIN) continue;
+            uint32_t n = scan_block(l, i, &blk, NULL);
+            if (!n) continue;
+            (void)scan_block(l, i, &blk, verts + first);
+            blk.first = first;
+            first += n;
+            blocks[nb++] = blk;
+            i = blk.end;
+        }
+        if (mtgl_dev_buffer_create(c->dev, &vb) != MTGL_OK) vb = 0;
+        if (vb && mtgl_dev_buffer_data(c->dev, vb, verts, nverts * sizeof(fe_vertex)) != MTGL_OK) {
+            (void)mtgl_dev_buffer_destroy(c->dev, vb);
+            vb = 0;
+        }
+    }
+    free(verts);
+    if (!vb) {
+        free(blocks);
+        return;
+    }
+    l->vb = vb;
+    l->blocks = blocks;
+    l->nblocks = nblocks;
+}
+
 /* list_alloc_range (lists.c:59-120) */
 GLuint glGenLists(GLsizei range)
 {
@@ -93,8 +224,7 @@ GLuint glGenLists(GLsizei range)
             if (++run >= (size_t)range) {
                 for (GLsizei k = 0; k < range; k++) {
                     fe_list *l = &c->lists[start + k];
-                    free(l->cmds);
-                    memset(l, 0, sizeof(*l));
+                    clear_list(c, l);
                     l->allocated = 1;
                 }
                 return (GLuint)(start + 1);
@@ -134,8 +264,7 @@ void glDeleteLists(GLuint list, GLsizei range)
     for (GLsizei i = 0; i < range; i++) {
         fe_list *l = fe_list_get(fe_ctx, list + (GLuint)i);
         if (!l) continue;
-        free(l->cmds);
-        memset(l, 0, sizeof(*l));
+        clear_list(fe_ctx, l);
     }
 }
 
@@ -156,6 +285,7 @@ void glNewList(GLuint list, GLenum mode)
         fe_set_error(c, GL_INVALID_VALUE);
         return;
     }
+    drop_blocks(c, l);
     l->count = 0;
     l->valid = 0;
     c->list_index = list;
@@ -174,6 +304,7 @@ void glEndList(void)
     if (l) l->valid = 1;
     c->list_index = 0;
     c->list_mode = 0;
+    if (l) build_blocks(c, l);
 }
 
 /* execute_list (gl_api.c:2331-2439) */
@@ -181,13 +312,21 @@ static void execute_list(GLuint id)
 {
     fe_list *l = fe_list_get(fe_ctx, id);
     if (!l || !l->valid) return;
+    size_t k = 0;  /* next device-resident block */
     for (size_t i = 0; i < l->count; i++) {
         /* re-fetch each step: a replayed call may grow another list's storage */
         l = fe_list_get(fe_ctx, id);
         if (!l || i >= l->count) return;
         fe_list_cmd cmd = l->cmds[i];
         switch (cmd.op) {
-        case LC_BEGIN: glBegin(cmd.e[0]); break;
+        case LC_BEGIN:
+            while (k < l->nblocks && l->blocks[k].begin < i) k++;
+            if (k < l->nblocks && l->blocks[k].begin == i && fe_draw_list_block(fe_ctx, l->vb, &l->blocks[k])) {
+                i = l->blocks[k].end;
+                break;
+            }
+            glBegin(cmd.e[0]);
+            break;
         case LC_END: glEnd(); break;
         case LC_VERTEX: glVertex3f(cmd.f[0], cmd.f[1], cmd.f[2]); break;
         case LC_COLOR: glColor4f(cmd.f[0], cmd.f[1], cmd.f[2], cmd.f[3]); break;

@@ -84,7 +84,7 @@ def _ptr(x):
 class Stats(ctypes.Structure):
     """mtgl_stats (include/mytinygl/mtgl_dev.h)"""
     _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "input_triangles", "setup_triangles", "bin_entries",
-                                               "fragments", "passes", "kernel_launches")]
+                                               "fragments", "passes", "kernel_launches", "staged_bytes")]
 
 
 class BatchConfig(ctypes.Structure):
@@ -162,6 +162,8 @@ class GLLibrary:
         L.mtgl_backend_name.argtypes = []
         L.mtgl_get_stats.restype = ctypes.c_int
         L.mtgl_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+        L.mtgl_reset_stats.restype = ctypes.c_int
+        L.mtgl_reset_stats.argtypes = [ctypes.c_void_p]
         self.has_player = hasattr(L, "mtgl_play")  # the reference build has none
         if self.has_player:
             L.mtgl_play.restype = ctypes.c_int
@@ -446,6 +448,9 @@ class GLContext:
         if st != 0:
             raise RuntimeError(f"mtgl_get_stats failed with status {st}")
         return {n: getattr(s, n) for n, _ in Stats._fields_}
+
+    def reset_stats(self):
+        self.glib.lib.mtgl_reset_stats(self.handle)
 
 
 _lib_cache: dict = {}

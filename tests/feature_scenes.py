@@ -8,8 +8,8 @@ quirk cases of the reference (alpha test only on textured fragments, stencil zpa
 the alpha test, flat shading from the clipped fan's last vertex, ...).
 
 Every scene clears every buffer it is compared on. `SCENES` maps a name to
-(builder, flags); flags: "lines" marks scenes that draw points/lines (a later GPU kernel),
-"slow" marks scenes too large for the golden set.
+(builder, flags); flags: "lines" marks scenes that draw points or lines, "slow" marks
+scenes too large for the golden set.
 """
 from __future__ import annotations
 
@@ -413,6 +413,104 @@ def sc_display_lists():
     return s
 
 
+def _block(s, rng, mode, n, color="each", uv=False, normal="each", z=(-6.0, -3.0), spread=1.6, two_d=False):
+    """One glBegin/glEnd block. color / normal: "each" (set before every vertex), "once"
+    (set before the first vertex only), "late" (set after the first vertex: the block takes
+    the caller's value first, so it must replay), None (never set: the caller's value)."""
+    s.glBegin(mode)
+    for k in range(n):
+        if color == "each" or (color == "once" and k == 0) or (color == "late" and k == 1):
+            s.glColor4f(*map(float, rng.uniform(0, 1, 4)))
+        if uv:
+            s.glTexCoord2f(*map(float, rng.uniform(-0.5, 1.5, 2)))
+        if normal == "each" or (normal == "once" and k == 0) or (normal == "late" and k == 1):
+            s.glNormal3f(*map(float, rng.uniform(-1, 1, 3)))
+        p = rng.uniform(-spread, spread, 3)
+        if two_d:
+            s.glVertex2f(float(p[0]), float(p[1]))
+        else:
+            s.glVertex3f(float(p[0]), float(p[1]), float(rng.uniform(*z)))
+    if color == "once" and n > 2:
+        s.glColor3f(0.2, 0.9, 0.4)  # after the last vertex: current afterwards, drawn by no vertex
+    s.glEnd()
+
+
+def sc_list_blocks():
+    """Display lists whose begin/end blocks are drawn from device-resident vertices, called
+    under changing matrices, current attributes and lighting; immediate draws after each call
+    take the current colour / texcoord / normal and the colour-material writes the calls left."""
+    s = base("list_blocks")
+    rng = np.random.default_rng(41)
+    checker_texture(s, size=8, seed=12)
+    s.glEnable(G.GL_DEPTH_TEST)
+    s.glGenLists(4)
+    s.glNewList(1, G.GL_COMPILE)
+    _block(s, rng, G.GL_TRIANGLES, 18, uv=True)
+    _block(s, rng, G.GL_TRIANGLE_FAN, 7, color=None, normal=None)
+    s.glPushMatrix()
+    s.glTranslatef(0.3, -0.2, -4.5)
+    _block(s, rng, G.GL_TRIANGLE_STRIP, 9, color="once", normal=None, two_d=True)
+    s.glPopMatrix()
+    _block(s, rng, G.GL_QUADS, 8, color="late")
+    _block(s, rng, G.GL_TRIANGLES, 0)
+    s.glEndList()
+    s.glNewList(2, G.GL_COMPILE)
+    _block(s, rng, G.GL_TRIANGLES, 15, color="once", normal="each")
+    _block(s, rng, G.GL_POLYGON, 6, color=None, normal="once")
+    _block(s, rng, G.GL_TRIANGLE_STRIP, 8, color="each", normal="late")
+    s.glEndList()
+    s.glNewList(3, G.GL_COMPILE)
+    s.glRotatef(20.0, 0.0, 0.0, 1.0)
+    s.glCallList(1)
+    _block(s, rng, G.GL_TRIANGLES, 9, color="each", uv=True, normal=None)
+    s.glEndList()
+
+    def immediate(n=3):
+        _block(s, rng, G.GL_TRIANGLES, n, color=None, normal=None, spread=2.0, z=(-7.0, -2.5))
+
+    s.glColor4f(0.9, 0.3, 0.2, 1.0)
+    s.glCallList(1)
+    immediate()
+    s.glTranslatef(0.4, 0.3, 0.0)
+    s.glColor4f(0.1, 0.5, 0.9, 0.5)
+    s.glEnable(G.GL_TEXTURE_2D)
+    s.glCallList(1)
+    immediate()
+    s.glDisable(G.GL_TEXTURE_2D)
+    s.glEnable(G.GL_LIGHTING)
+    s.glEnable(G.GL_LIGHT0)
+    s.glEnable(G.GL_COLOR_MATERIAL)
+    s.glNormal3f(0.0, 0.0, 1.0)
+    s.glCallList(2)
+    immediate()
+    s.glColorMaterial(G.GL_FRONT, G.GL_DIFFUSE)
+    s.glColor4f(0.8, 0.8, 0.1, 1.0)
+    s.glNormal3f(0.3, -0.5, 0.8)
+    s.glCallList(2)
+    s.glDisable(G.GL_COLOR_MATERIAL)
+    immediate()
+    s.glDisable(G.GL_LIGHTING)
+    # executed while another list is compiled: every block replays and is recorded
+    s.glNewList(4, G.GL_COMPILE_AND_EXECUTE)
+    s.glCallList(3)
+    s.glEndList()
+    s.glScalef(0.7, 0.7, 1.0)
+    s.glCallList(4)
+    immediate()
+    # a vertex emitted outside glBegin/glEnd is pending: the next block replays and takes it
+    s.glVertex3f(0.1, 0.2, -3.0)
+    s.glCallList(1)
+    immediate()
+    s.glDeleteLists(1, 1)
+    s.glCallList(3)
+    s.glNewList(2, G.GL_COMPILE)
+    _block(s, rng, G.GL_TRIANGLES, 6, color="each", normal=None)
+    s.glEndList()
+    s.glCallList(2)
+    immediate()
+    return s
+
+
 def sc_vertex_arrays():
     s = base("vertex_arrays")
     rng = np.random.default_rng(30)
@@ -744,6 +842,7 @@ SCENES = {
     "scissor_mask": (sc_scissor_mask, ()),
     "viewport": (sc_viewport, ()),
     "display_lists": (sc_display_lists, ()),
+    "list_blocks": (sc_list_blocks, ()),
     "vertex_arrays": (sc_vertex_arrays, ()),
     "vbo": (sc_vbo, ()),
     "state_in_begin_end": (sc_state_in_begin_end, ()),

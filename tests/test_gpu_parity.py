@@ -172,3 +172,71 @@ def test_depth_rejection_changes_nothing(gpu, which):
         outs.append(ctx.read() + (ctx.glGetError(),))
         ctx.destroy()
     harness.assert_parity(harness.compare(outs[0], outs[1]), color_tol=0, name=f"{which} rejection on/off")
+
+
+def _list_calls(ctx, rng_seed=5, late=False):
+    """A list of one 3,000-triangle block (colour and normal per vertex), called three times
+    under different modelviews and lighting."""
+    rng = np.random.default_rng(rng_seed)
+    n = 9000
+    pos = rng.uniform(-2.5, 2.5, (n, 3)).astype(np.float32)
+    pos[:, 2] = rng.uniform(-7.0, -2.0, n)
+    col = rng.uniform(0, 1, (n, 4)).astype(np.float32)
+    nrm = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    ctx.glViewport(0, 0, 160, 120)
+    ctx.glMatrixMode(G.GL_PROJECTION)
+    ctx.glLoadIdentity()
+    ctx.glFrustum(-0.4, 0.4, -0.3, 0.3, 0.5, 20.0)
+    ctx.glMatrixMode(G.GL_MODELVIEW)
+    ctx.glLoadIdentity()
+    ctx.glEnable(G.GL_DEPTH_TEST)
+    ctx.glClear(G.GL_COLOR_BUFFER_BIT | G.GL_DEPTH_BUFFER_BIT | G.GL_STENCIL_BUFFER_BIT)
+    ctx.glGenLists(1)
+    ctx.glNewList(1, G.GL_COMPILE)
+    ctx.glBegin(G.GL_TRIANGLES)
+    for i in range(n):
+        if not late or i > 0:
+            ctx.glColor4f(*map(float, col[i]))
+        ctx.glNormal3f(*map(float, nrm[i]))
+        ctx.glVertex3f(*map(float, pos[i]))
+    ctx.glEnd()
+    ctx.glEndList()
+    yield
+    ctx.glCallList(1)
+    ctx.glRotatef(25.0, 0.2, 0.3, 1.0)
+    ctx.glEnable(G.GL_LIGHTING)
+    ctx.glEnable(G.GL_LIGHT0)
+    ctx.glEnable(G.GL_COLOR_MATERIAL)
+    ctx.glCallList(1)
+    ctx.glTranslatef(0.5, -0.3, -1.0)
+    ctx.glDisable(G.GL_COLOR_MATERIAL)
+    ctx.glCallList(1)
+
+
+@pytest.mark.parametrize("late", [False, True], ids=["resident", "replayed"])
+def test_list_block_device_resident(gpu, oracle, late):
+    """glCallList draws a qualifying block from the list's device buffer: no client bytes
+    are staged for it, and the frame matches the oracle. A block that sets its colour after
+    a vertex has taken the caller's replays through immediate mode and stages its vertices."""
+    out = []
+    for lib in (oracle, gpu):
+        ctx = lib.context(160, 120)
+        ctx.make_current()
+        steps = _list_calls(ctx, late=late)
+        next(steps)
+        ctx.finish()
+        if lib is gpu:
+            ctx.reset_stats()
+        for _ in steps:
+            pass
+        out.append(ctx.read())
+        if lib is gpu:
+            st = ctx.stats()
+            if late:
+                assert st["staged_bytes"] >= 3 * 9000 * 48
+            else:
+                assert st["staged_bytes"] == 0
+            assert st["input_triangles"] == 3 * 3000
+        ctx.destroy()
+    stats = harness.compare(out[0] + (0,), out[1] + (0,))
+    harness.assert_parity(stats, color_tol=1, name="list_block")

@@ -185,6 +185,11 @@ int mtgl_dev_draw_pixels(mtgl_dev *d, int32_t raster_x, int32_t raster_y, int32_
 /* ---- synchronisation and readback ---- */
 int mtgl_dev_flush(mtgl_dev *d);   /* submit queued work; returns without waiting        */
 int mtgl_dev_finish(mtgl_dev *d);  /* submit and wait                                    */
+/* 1 while a batch that writes this context's framebuffer or reads its resources has not
+ * been waited for (by mtgl_dev_batch_wait, or by an operation of the context that needs
+ * it), else 0. A context at 0 shares no host state with other contexts until it joins a
+ * batch, so distinct such contexts can be driven from distinct threads (mtgl_play_many). */
+int mtgl_dev_in_batch(const mtgl_dev *d);
 /* Finish, then copy whole buffers (row 0 = top) to host memory; any pointer may be NULL. */
 int mtgl_dev_read(mtgl_dev *d, uint32_t *color, float *depth, uint8_t *stencil);
 int mtgl_dev_stats(mtgl_dev *d, mtgl_stats *out);

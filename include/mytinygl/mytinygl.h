@@ -70,6 +70,11 @@ int mtgl_flush_noalloc(GLState *ctx);
  * up exactly as mtgl_finish on each context alone would leave it. Returns without
  * waiting; reading a context (glReadPixels, glFinish, mtgl_color_buffer) waits for it. */
 int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n);
+/* mtgl_batch_render, then after the run a copy of each context's colour buffer (width*height
+ * packed RGBA8, row 0 = top) into colors[i]; NULL entries (or a NULL colors) copy nothing.
+ * The copies have landed when mtgl_dev_batch_wait returns; page-locked destinations keep
+ * them asynchronous. */
+int mtgl_batch_render_read(mtgl_batch *b, GLState *const *ctxs, uint32_t *const *colors, int32_t n);
 
 /* Replay a GL command stream onto ctx (made current). No counterpart in the reference.
  * The stream is a sequence of records: u32 function id (the entry point's index among the
@@ -79,7 +84,12 @@ int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n);
  * pointers must stay valid for as long as GL may read them. Returns MTGL_ERR_INVALID at
  * the first malformed record (the calls before it have run). */
 int mtgl_play(GLState *ctx, const void *stream, size_t bytes);
-/* mtgl_play for each (ctxs[i], streams[i]) in order; the current context is restored. */
+/* mtgl_play for each (ctxs[i], streams[i]). When the contexts are distinct and in no
+ * unfinished batch, the streams play concurrently on a pool of host threads
+ * (MTGL_PLAY_THREADS, default: the online cores), each context on one thread; otherwise in
+ * order on the calling thread. Every
+ * stream is played; returns the status of the first failing stream by index. The calling
+ * thread's current context is restored. */
 int mtgl_play_many(GLState *const *ctxs, const void *const *streams, const size_t *bytes, int32_t n);
 /* number of entry points a stream can call (the function-id range) */
 int mtgl_play_function_count(void);

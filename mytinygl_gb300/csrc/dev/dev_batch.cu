@@ -60,6 +60,10 @@ struct mtgl_batch {
     std::vector<Pass> passes;
     std::vector<FrameSrc> frames;     // frame f renders passes[f] into frames[f].dev
     std::vector<std::pair<mtgl_dev *, uint32_t *>> readbacks;
+    // client bytes of the first passes go to the device copy at add time, straight from
+    // their context's pinned staging area; the rest are copied into this batch's area
+    size_t direct_end = 0;
+    bool direct_ok = true;
     uint64_t open_tris = 0;
     bool ran = false;                 // the pending submission ran the pipeline (not readbacks only)
     Tables t;
@@ -231,6 +235,8 @@ int mtgl_dev_batch_begin(mtgl_batch *b)
     b->passes.clear();
     b->frames.clear();
     b->readbacks.clear();
+    b->direct_end = 0;
+    b->direct_ok = true;
     b->open_tris = 0;
     b->open = true;
     return MTGL_OK;
@@ -303,8 +309,18 @@ int mtgl_dev_batch_add(mtgl_batch *b, mtgl_dev *src, mtgl_dev *target)
     int st;
     if ((st = involve(b, src, src == target)) || (st = involve(b, target, true))) return st;
     int64_t off = 0;
-    if ((st = b->stage.reserve(src->stage.used, &off))) return st;
-    if (src->stage.used) memcpy(b->stage.p + off, src->stage.p, src->stage.used);
+    const size_t bytes = src->stage.used;
+    if ((st = b->stage.reserve(bytes, &off))) return st;
+    if (bytes && b->direct_ok && (size_t)off + bytes <= b->x.dcap) {
+        // The batch stream runs this copy after the batch's previous run and before this
+        // one; the context's next staging write waits for it.
+        CK(cudaMemcpyAsync(b->x.dstage + off, src->stage.p, bytes, cudaMemcpyHostToDevice, b->x.stream));
+        if ((st = src->stage.mark_uploaded(b->x.stream))) return st;
+        b->direct_end = (size_t)off + bytes;
+    } else if (bytes) {
+        b->direct_ok = false;  // offsets only grow: later passes do not fit either
+        memcpy(b->stage.p + off, src->stage.p, bytes);
+    }
     b->passes.push_back(std::move(src->pass));
     src->pass.reset();
     src->stage.used = 0;
@@ -339,7 +355,8 @@ int mtgl_dev_batch_launch(mtgl_batch *b)
         return MTGL_OK;
     }
     for (size_t i = 0; i < b->frames.size(); i++) b->frames[i].pass = &b->passes[i];
-    if ((st = build_tables(b->x, b->stage, b->frames.data(), (uint32_t)b->frames.size(), b->tile_shift, true, b->t)))
+    if ((st = build_tables(b->x, b->stage, b->frames.data(), (uint32_t)b->frames.size(), b->tile_shift, true, b->t,
+                           b->direct_end)))
         return st;
     const uint64_t tris = b->open_tris;
     // capacities: the larger of the learned totals and the configured factors
@@ -366,7 +383,9 @@ int mtgl_dev_batch_launch(mtgl_batch *b)
     return MTGL_OK;
 }
 
-int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
+// every context renders its own pending pass; colors[i] (when given and non-null) receives
+// devs[i]'s colour buffer after the run
+static int submit_read(mtgl_batch *b, mtgl_dev *const *devs, uint32_t *const *colors, int32_t n)
 {
     if (!b || n < 0 || (n > 0 && !devs)) return MTGL_ERR_INVALID;
     for (int32_t i = 0; i < n; i++) {
@@ -382,8 +401,16 @@ int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n)
             return st;
         }
     }
+    for (int32_t i = 0; colors && i < n; i++) {
+        if (colors[i] && (st = mtgl_dev_batch_readback(b, devs[i], colors[i]))) {
+            b->open = false;
+            return st;
+        }
+    }
     return mtgl_dev_batch_launch(b);
 }
+
+int mtgl_dev_batch_submit(mtgl_batch *b, mtgl_dev *const *devs, int32_t n) { return submit_read(b, devs, nullptr, n); }
 
 int mtgl_dev_batch_query(mtgl_batch *b)
 {
@@ -498,7 +525,7 @@ int mtgl_dev_batch_timings(mtgl_batch *b, mtgl_timings *out)
 
 extern "C" mtgl_dev *fe_context_device(GLState *ctx);
 
-extern "C" int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n)
+extern "C" int mtgl_batch_render_read(mtgl_batch *b, GLState *const *ctxs, uint32_t *const *colors, int32_t n)
 {
     if (!b || n < 0 || (n > 0 && !ctxs)) return MTGL_ERR_INVALID;
     std::vector<mtgl_dev *> devs((size_t)n);
@@ -506,5 +533,10 @@ extern "C" int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n)
         devs[i] = ctxs[i] ? fe_context_device(ctxs[i]) : nullptr;
         if (!devs[i]) return MTGL_ERR_INVALID;
     }
-    return mtgl_dev_batch_submit(b, devs.data(), n);
+    return submit_read(b, devs.data(), colors, n);
+}
+
+extern "C" int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n)
+{
+    return mtgl_batch_render_read(b, ctxs, nullptr, n);
 }

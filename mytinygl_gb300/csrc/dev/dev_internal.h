@@ -120,7 +120,7 @@ struct Exec {
 
     int init(cudaStream_t s);  // s null: create a stream
     void destroy();
-    int ensure_dstage(size_t bytes, bool may_grow);
+    int ensure_dstage(size_t bytes, bool may_grow, size_t keep = 0);  // keep: leading bytes that survive growth
     void prof_mark();
     int prof_collect();  // the caller has synchronised the stream
 };
@@ -136,6 +136,7 @@ struct FrameSrc {
 // The tables of a pass inside the staging area (offsets are the same in the host copy and
 // in the device copy).
 struct Tables {
+    int64_t off_upload = 0;  // staged bytes before this offset are already in the device copy
     int64_t off_draws = 0, off_vbase = 0, off_tbase = 0, off_vs = 0, off_rs = 0, off_clears = 0, off_frames = 0;
     uint32_t ndraws = 0, nrasters = 0, nclears = 0, nframes = 0;
     uint32_t slots = 0, tris = 0, ntiles = 0;
@@ -144,8 +145,10 @@ struct Tables {
 };
 
 // Appends the tables of `frames` to `st` and makes the device staging copy large enough.
+// `direct`: the first bytes of the area were copied to the device copy already (the upload
+// starts after them, and they survive a growth of the device copy).
 int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframes, int tile_shift, bool may_grow,
-                 Tables &t);
+                 Tables &t, size_t direct = 0);
 
 // CTAs of a persistent tile launch for these tables: per_sm per SM (0: all that fit)
 int persistent_ctas(const Exec &x, const Tables &t, int per_sm);
@@ -164,7 +167,7 @@ struct PipeOut {
     int launches = 0;
 };
 
-// Uploads st[0, st.used) and runs K1..K4 on x.stream. Capacity mode enqueues only (no host
+// Uploads st[t.off_upload, st.used) and runs K1..K4 on x.stream. Capacity mode enqueues only (no host
 // waits and no allocation after its first step), so it can be captured into a CUDA graph;
 // alloc_only makes it take its scratch and return without enqueueing anything.
 int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &t, const PipeConfig &c,

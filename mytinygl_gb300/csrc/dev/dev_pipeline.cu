@@ -158,7 +158,7 @@ void Exec::destroy()
     h_totals = nullptr;
 }
 
-int Exec::ensure_dstage(size_t bytes, bool may_grow)
+int Exec::ensure_dstage(size_t bytes, bool may_grow, size_t keep)
 {
     if (bytes <= dcap) return MTGL_OK;
     if (!may_grow) {
@@ -166,10 +166,11 @@ int Exec::ensure_dstage(size_t bytes, bool may_grow)
         return MTGL_ERR_OVERFLOW;
     }
     const size_t cap = std::max(bytes, dcap * 2);
+    uint8_t *n = nullptr;
+    CK(cudaMallocAsync((void **)&n, cap, stream));
+    if (dstage && keep) CK(cudaMemcpyAsync(n, dstage, std::min(keep, dcap), cudaMemcpyDeviceToDevice, stream));
     if (dstage) CK(cudaFreeAsync(dstage, stream));
-    dstage = nullptr;
-    dcap = 0;
-    CK(cudaMallocAsync((void **)&dstage, cap, stream));
+    dstage = n;
     dcap = cap;
     return MTGL_OK;
 }
@@ -208,9 +209,10 @@ int Exec::prof_collect()
 // ------------------------------------------------------------------ tables
 
 int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframes, int tile_shift, bool may_grow,
-                 Tables &t)
+                 Tables &t, size_t direct)
 {
     t = Tables();
+    t.off_upload = (int64_t)direct;
     t.tile_shift = tile_shift;
     t.nframes = nframes;
     size_t ndraws = 0, nvs = 0, nrs = 0, ncl = 0;
@@ -242,7 +244,7 @@ int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframe
         (s = st.reserve(std::max<size_t>(1, nrs) * sizeof(DevRaster), &t.off_rs)) ||
         (s = st.reserve(std::max<size_t>(1, ncl) * sizeof(ClearOp), &t.off_clears)) ||
         (s = st.reserve(std::max<uint32_t>(1, nframes) * sizeof(DevFrame), &t.off_frames)) ||
-        (s = x.ensure_dstage(st.used, may_grow))) {
+        (s = x.ensure_dstage(st.used, may_grow, direct))) {
         st.used = used0;
         return s;
     }
@@ -373,7 +375,8 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if ((rc = sc.take(S_SCAN_TEMP, scan_temp_words(scan_n), &scan_temp))) return rc;
     if (alloc_only) return MTGL_OK;
 
-    CK(cudaMemcpyAsync(ds, st.p, st.used, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ds + t.off_upload, st.p + t.off_upload, st.used - (size_t)t.off_upload, cudaMemcpyHostToDevice,
+                       s));
     x.prof_mark();
 
     GeomArgs ga;

@@ -514,6 +514,8 @@ int mtgl_dev_finish(mtgl_dev *d)
     return MTGL_OK;
 }
 
+int mtgl_dev_in_batch(const mtgl_dev *d) { return d && (d->batch || !d->readers.empty()) ? 1 : 0; }
+
 int mtgl_dev_read(mtgl_dev *d, uint32_t *color, float *depth, uint8_t *stencil)
 {
     if (!d) return MTGL_ERR_INVALID;

@@ -144,17 +144,6 @@ def generate() -> str:
         "    return MTGL_OK;",
         "}",
         "",
-        "int mtgl_play_many(GLState *const *ctxs, const void *const *streams, const size_t *bytes, int32_t n)",
-        "{",
-        "    GLState *prev = gl_get_current_context();",
-        "    int32_t i;",
-        "    int st = MTGL_OK;",
-        "    if (n < 0 || (n > 0 && (!ctxs || !streams || !bytes))) return MTGL_ERR_INVALID;",
-        "    for (i = 0; i < n && st == MTGL_OK; i++) st = mtgl_play(ctxs[i], streams[i], bytes[i]);",
-        "    gl_make_current(prev);",
-        "    return st;",
-        "}",
-        "",
     ]
     return "\n".join(lines)
 

@@ -81,6 +81,11 @@ def _ptr(x):
     return int(x)
 
 
+def _nbytes(x):
+    """Size of a destination array (raw addresses are taken on trust)."""
+    return x.nbytes if isinstance(x, np.ndarray) else 1 << 62
+
+
 class Stats(ctypes.Structure):
     """mtgl_stats (include/mytinygl/mtgl_dev.h)"""
     _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "input_triangles", "setup_triangles", "bin_entries",
@@ -213,6 +218,9 @@ class GLLibrary:
         L.mtgl_dev_batch_stream.argtypes = [ctypes.c_void_p]
         L.mtgl_batch_render.restype = ctypes.c_int
         L.mtgl_batch_render.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]
+        L.mtgl_batch_render_read.restype = ctypes.c_int
+        L.mtgl_batch_render_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                                             ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]
 
     @property
     def backend(self) -> str:
@@ -329,9 +337,22 @@ class Batch:
             raise RuntimeError(f"mtgl_dev_batch_create failed with status {st}")
         self.handle = h.value
 
-    def render(self, contexts):
-        arr = (ctypes.c_void_p * len(contexts))(*[c.handle for c in contexts])
-        st = self.glib.lib.mtgl_batch_render(self.handle, arr, len(contexts))
+    def render(self, contexts, colors=None):
+        """mtgl_batch_render; with `colors` (one host array or None per context, uint32
+        [height, width], page-locked for asynchronous copies: mtgl_batch_render_read), each
+        listed colour buffer is copied out after the run (landed when wait() returns)."""
+        n = len(contexts)
+        arr = (ctypes.c_void_p * n)(*[c.handle for c in contexts])
+        if colors is None:
+            st = self.glib.lib.mtgl_batch_render(self.handle, arr, n)
+        else:
+            if len(colors) != n:
+                raise ValueError("one colour destination (or None) per context")
+            for c, h in zip(contexts, colors):
+                if h is not None and _nbytes(h) < 4 * c.width * c.height:
+                    raise ValueError("colour destination smaller than the framebuffer")
+            dst = (ctypes.c_void_p * n)(*[_ptr(h) if h is not None else None for h in colors])
+            st = self.glib.lib.mtgl_batch_render_read(self.handle, arr, dst, n)
         if st != 0:
             raise RuntimeError(f"mtgl_batch_render failed with status {st}")
 

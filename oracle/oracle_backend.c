@@ -1338,6 +1338,7 @@ int mtgl_dev_draw_pixels(mtgl_dev *d, int32_t rx, int32_t ry, int32_t width, int
 
 int mtgl_dev_flush(mtgl_dev *d) { (void)d; return MTGL_OK; }
 int mtgl_dev_finish(mtgl_dev *d) { (void)d; return MTGL_OK; }
+int mtgl_dev_in_batch(const mtgl_dev *d) { (void)d; return 0; }
 
 int mtgl_dev_read(mtgl_dev *d, uint32_t *color, float *depth, uint8_t *stencil)
 {
@@ -1500,4 +1501,12 @@ int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n)
     b->stats.batches++;
     b->stats.frames += (uint64_t)n;
     return MTGL_OK;
+}
+
+int mtgl_batch_render_read(mtgl_batch *b, GLState *const *ctxs, uint32_t *const *colors, int32_t n)
+{
+    int st = mtgl_batch_render(b, ctxs, n);
+    for (int32_t i = 0; st == MTGL_OK && colors && i < n; i++)
+        if (colors[i]) st = mtgl_read_framebuffer(ctxs[i], colors[i], NULL, NULL);
+    return st;
 }

@@ -159,3 +159,26 @@ def test_context_reused_after_batch(gpu, oracle):
     harness.assert_parity(harness.compare(want, got), 1, "reused")
     for x in ctxs + [ctx, ref]:
         x.destroy()
+
+
+def test_render_read_with_direct_uploads(gpu):
+    """Client-array frames through mtgl_batch_render_read over several rounds: the first
+    round copies the frames' staged bytes into the batch's staging area, later rounds send
+    them straight from each context's staging area (round three adds frames past the device
+    copy's size, which then grows keeping what was sent). Colour copied out by the batch
+    equals what the plain path renders, every round."""
+    scenes = W.uneven_batch(18, seed=15, min_side=16, max_side=160, min_tri=20, max_tri=2500, tex_size=32,
+                            use_vbo=False)
+    want = plain(gpu, scenes)
+    ctxs, streams = setup_frames(gpu, scenes)
+    b = gpu.batch(tile_size=16)
+    for k in (6, 6, 18, 18):
+        hosts = [np.zeros((s.height, s.width), np.uint32) for s in scenes[:k]]
+        gpu.play_many(ctxs[:k], streams[:k])
+        b.render(ctxs[:k], colors=hosts)
+        b.wait()
+        for h, w, s in zip(hosts, want, scenes):
+            assert np.array_equal(h, w[0]), f"{s.name} (batch of {k})"
+    b.destroy()
+    for c in ctxs:
+        c.destroy()

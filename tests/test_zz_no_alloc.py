@@ -22,26 +22,19 @@ pytestmark = pytest.mark.gpu
 MTGL_ERR_OVERFLOW = 7
 
 
-class Stats(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_uint64) for n in
-                ("draws", "input_triangles", "setup_triangles", "bin_entries", "fragments", "passes", "kernel_launches")]
-
-
 @pytest.fixture(scope="module")
 def gpu():
     lib = harness.product()
     L = lib.lib
     L.mtgl_flush_noalloc.argtypes = [ctypes.c_void_p]
     L.mtgl_flush_noalloc.restype = ctypes.c_int
-    L.mtgl_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
-    L.mtgl_get_stats.restype = ctypes.c_int
     return lib
 
 
 def passes(ctx):
     """Passes rendered so far. Reading the counters waits for the context, so it also
     renders anything still queued: call it only when nothing should be."""
-    s = Stats()
+    s = G.Stats()
     assert ctx.glib.lib.mtgl_get_stats(ctx.handle, ctypes.byref(s)) == 0
     return int(s.passes)
 

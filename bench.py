@@ -205,6 +205,28 @@ def dist_init():
     return world, rank, local
 
 
+def max_over_ranks(x, device="cuda"):
+    """The largest x over the ranks of the process group (x itself without one)."""
+    import torch
+
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units, seconds, device="cuda"):
+    """Whole-job throughput of replicas: each of the world's ranks processes `units` in its
+    own `seconds`; the job takes as long as its slowest rank."""
+    import torch
+
+    world = 1
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        world = torch.distributed.get_world_size()
+    return world * units / max_over_ranks(seconds, device)
+
+
 def run_ours(args, spec):
     import torch
 
@@ -256,11 +278,7 @@ def run_ours(args, spec):
     tm = Timings()
     ctx.glib.lib.mtgl_get_timings(ctx.handle, ctypes.byref(tm))
     ctx.glib.lib.mtgl_set_profiling(ctx.handle, 0)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    fps = world * args.steps / (total_ms / 1e3)
+    fps = job_rate(args.steps, total_ms / 1e3)
     tested_per_frame = st["fragments"] / args.steps
     ctx.destroy()
     frags_per_frame = covered_fragments(lib, scene, fs)
@@ -285,7 +303,7 @@ def run_ours(args, spec):
     efs = W.frame_start(escene)
     ectx = lib.context(escene.width, escene.height)
     escene.play(ectx, 0, efs)
-    host = np.empty((escene.height, escene.width), np.uint32)
+    host = torch.empty((escene.height, escene.width), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     for _ in range(args.warmup):
         escene.play(ectx, efs)
         ectx.read(color=True, depth=False, stencil=False)
@@ -295,7 +313,7 @@ def run_ours(args, spec):
         ectx.glib.lib.mtgl_read_framebuffer(ectx.handle, host.ctypes.data, None, None)
     e2e_s = time.perf_counter() - t0
     ectx.destroy()
-    e2e_fps = world * args.steps / e2e_s
+    e2e_fps = job_rate(args.steps, e2e_s)
     h2d = scene_bytes(escene, efs)
     d2h = escene.width * escene.height * 4
 
@@ -417,11 +435,7 @@ def run_batch(args, spec):
         wall = time.perf_counter() - t0
     total_ms = sum(s_.elapsed_time(e) for s_, e in zip(starts, ends))
     bst = batch.stats()
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    fps = world * args.steps * BATCH_FRAMES / (total_ms / 1e3)
+    fps = job_rate(args.steps * BATCH_FRAMES, total_ms / 1e3)
 
     # host clock, outside the clock sampler (its NVML queries stall the driver): the batched
     # path and the plain per-frame path (each frame's pass flushed on its own context, as
@@ -433,7 +447,7 @@ def run_batch(args, spec):
         streams.play()
         batch.render(ctxs)
     batch.wait()
-    batched_wall_fps = wall_steps * BATCH_FRAMES / (time.perf_counter() - t0)
+    batched_wall_fps = job_rate(wall_steps * BATCH_FRAMES, time.perf_counter() - t0)
     for c in ctxs:
         c.glFinish()
     plain_fps = {}
@@ -445,7 +459,7 @@ def run_batch(args, spec):
                 c.glFinish() if mode == "finish" else c.glFlush()
             for c in ctxs:
                 c.glFinish()
-        plain_fps[mode] = max(1, wall_steps // 2) * BATCH_FRAMES / (time.perf_counter() - t0)
+        plain_fps[mode] = job_rate(max(1, wall_steps // 2) * BATCH_FRAMES, time.perf_counter() - t0)
     plain_best = max(plain_fps.values())
 
     # per-phase device time from a profiled run without the graph (K4 roofline)
@@ -516,6 +530,8 @@ def run_batch(args, spec):
     for _, _, ebatch, _ in sets:
         ebatch.wait()
     e2e_s = time.perf_counter() - t0
+    e2e_fps = job_rate(e_steps * BATCH_FRAMES, e2e_s)
+    e2e_seq_fps = job_rate(e_steps * BATCH_FRAMES, e2e_seq_s)
     for ectxs, _, ebatch, _ in sets:
         ebatch.destroy()
         for c in ectxs:
@@ -561,9 +577,9 @@ def run_batch(args, spec):
                      "peak_source": f"{peak_src} (HBM copy)", "unit": "GB/s",
                      "frac": round(achieved / peak, 5) if achieved else None,
                      "algorithmic_bytes_per_launch": int(k4_bytes), "traffic": ncu_traffic(spec["name"])},
-        "e2e": {"value": round(e_steps * BATCH_FRAMES / e2e_s, 2), "unit": "frames/s",
+        "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(npix * 4), "steps_in_flight": 2,
-                "sequential_value": round(e_steps * BATCH_FRAMES / e2e_seq_s, 2),
+                "sequential_value": round(e2e_seq_fps, 2),
                 "note": "host clock; GL calls replayed with client arrays every step (their staged bytes are "
                         "h2d), every colour buffer copied to page-locked host memory"},
         "gpu_launches": int(bst["kernel_launches"]),
@@ -594,7 +610,7 @@ def _latency_summary(reqs):
     return {"p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
             "mean_ms": round(float(lat.mean()), 3), "max_ms": round(float(lat.max()), 3),
             "completed": len(ok), "failed": len(reqs) - len(ok),
-            "frames_per_s": round(len(ok) / span, 2),
+            "frames_per_s": round(len(ok) / span, 2), "span_s": span,
             "mean_batch": round(float(np.mean([r.batch_size for r in ok])), 2)}
 
 
@@ -609,6 +625,8 @@ def run_serve(args, spec):
 
     world, rank, local = dist_init()
     torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     import mytinygl_gb300 as M
 
     M.build()
@@ -635,6 +653,7 @@ def run_serve(args, spec):
         srv.run_trace(reqs)
         st1 = srv.stats()
     summ = _latency_summary(reqs)
+    served_fps = job_rate(summ["completed"], summ["span_s"])
     busy = st1["busy_seconds"] - st0["busy_seconds"]
     batches = st1["batches"] - st0["batches"]
     # the rated load saturates the GPU: latency there is mostly queueing. Latency below
@@ -661,12 +680,13 @@ def run_serve(args, spec):
     ereqs = _serve_requests(etrace, srv.now() + 0.05, out_for)
     srv.run_trace(ereqs)
     esumm = _latency_summary(ereqs)
+    e2e_fps = job_rate(esumm["completed"], esumm["span_s"])
     d2h = sum(w * h * 4 for _, _, w, h, _ in etrace) / max(1, len(etrace))
     srv.destroy()
     for c in ctxs:
         c.destroy()
     out = {
-        "metric": "frames/s", "value": summ["frames_per_s"], "unit": "frames/s", "n_gpus": world,
+        "metric": "frames/s", "value": round(served_fps, 2), "unit": "frames/s", "n_gpus": world,
         "steps": len(reqs), "warmup": args.warmup, "ms_per_step": summ["mean_ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; mytinygl_gb300/workloads.py serve_scenes / serve_trace)",
@@ -682,9 +702,9 @@ def run_serve(args, spec):
         "gpu_busy_fraction": round(busy / max(1e-9, max(r.finished for r in reqs) - min(r.arrival for r in reqs)), 3),
         "deferred_for_budget": st1["deferred_for_budget"] - st0["deferred_for_budget"],
         "peak_gib_admitted": round(st1["peak_bytes_admitted"] / 2**30, 3),
-        "e2e": {"value": esumm["frames_per_s"], "unit": "frames/s", "h2d_bytes_per_step": 0,
+        "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(d2h), "latency_ms": {"p50": esumm["p50_ms"], "p99": esumm["p99_ms"]}},
-        "gpu_launches": None, "clocks": clocks.summary(),
+        "gpu_launches": int(st1["kernel_launches"] - st0["kernel_launches"]), "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -693,6 +713,8 @@ def run_serve(args, spec):
                                "cores": threads, "kind": "port",
                                "sample": (f"{len(times)} requests of the trace, each frame on its own oracle "
                                           f"context, {threads} threads; frames/s = threads / mean frame time")}
+    if world > 1:
+        torch.distributed.destroy_process_group()
     return out if rank == 0 else None
 
 

@@ -60,6 +60,7 @@ typedef struct {
     uint64_t submitted, completed, failed, batches, deferred_for_budget;
     uint64_t peak_bytes_admitted, framebuffers_allocated;
     double busy_seconds;       /* time with at least one batch in flight                             */
+    uint64_t kernel_launches;  /* device kernels the completed batches launched                      */
 } mtgl_server_stats;
 
 int mtgl_server_create(const mtgl_server_config *cfg, mtgl_server **out);

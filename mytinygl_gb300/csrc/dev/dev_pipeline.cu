@@ -1,6 +1,8 @@
 // dev_pipeline.cu — the pass pipeline shared by single-context flushes and batches:
 // staging helpers, scratch, table assembly and the K1 -> K2 -> K3 -> K4 launch sequence.
 #include <algorithm>
+#include <atomic>
+#include <thread>
 
 #include "dev_internal.h"
 
@@ -49,11 +51,44 @@ int HostStage::reserve(size_t bytes, int64_t *off)
     return MTGL_OK;
 }
 
+// One core copies into pinned memory at a fraction of what host memory and the link to the
+// GPU sustain, so a large client array is copied by several threads at once. One such copy
+// runs at a time; a copy that finds another running (contexts on several threads) copies
+// alone.
+static std::atomic<bool> g_par_copy_busy{false};
+
+static void par_copy(uint8_t *dst, const uint8_t *src, size_t bytes)
+{
+    const size_t kMin = (size_t)8 << 20, kPiece = (size_t)2 << 20;
+    const unsigned hc = std::thread::hardware_concurrency();
+    bool idle = false;
+    if (bytes < kMin || hc < 2 || !g_par_copy_busy.compare_exchange_strong(idle, true)) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t n = std::min<size_t>(std::min<size_t>(hc, 8), bytes / kPiece);
+    const size_t per = (bytes / n + 63) & ~(size_t)63;
+    std::vector<std::thread> helpers;
+    size_t done = std::min(per, bytes);  // this thread's piece
+    try {
+        for (size_t a = per; a < bytes; a += per) {
+            const size_t len = std::min(per, bytes - a);
+            helpers.emplace_back([=] { memcpy(dst + a, src + a, len); });
+            done = a + len;
+        }
+    } catch (...) {  // no thread to be had: copy the rest here
+    }
+    memcpy(dst, src, std::min(per, bytes));
+    if (done < bytes) memcpy(dst + done, src + done, bytes - done);
+    for (std::thread &t : helpers) t.join();
+    g_par_copy_busy.store(false);
+}
+
 int HostStage::copy(const void *src, size_t bytes, int64_t *off)
 {
     int st = reserve(bytes, off);
     if (st) return st;
-    if (bytes) memcpy(p + *off, src, bytes);
+    if (bytes) par_copy(p + *off, static_cast<const uint8_t *>(src), bytes);
     return MTGL_OK;
 }
 

@@ -49,6 +49,7 @@ typedef struct {
 
 typedef struct {
     mtgl_batch *b;
+    uint64_t launches_seen; /* the batch's kernel_launches counter at its last completion */
     int pending;
     int n;
     mtgl_request **reqs;
@@ -158,6 +159,13 @@ static int complete_batches(mtgl_server *s)
         int q = mtgl_dev_batch_query(e->b);
         if (q == 0) continue;
         int st = q < 0 ? -q : mtgl_dev_batch_wait(e->b);
+        mtgl_batch_stats bs;
+        if (mtgl_dev_batch_stats(e->b, &bs) == MTGL_OK) {
+            pthread_mutex_lock(&s->mu);
+            s->st.kernel_launches += bs.kernel_launches - e->launches_seen;
+            pthread_mutex_unlock(&s->mu);
+            e->launches_seen = bs.kernel_launches;
+        }
         e->pending = 0;
         for (j = 0; j < e->n; j++) {
             e->slots[j]->busy = 0;
@@ -167,7 +175,12 @@ static int complete_batches(mtgl_server *s)
         e->n = 0;
         done = 1;
     }
-    if (done && !any_pending(s)) s->st.busy_seconds += elapsed(&s->t0) - s->busy_since;
+    if (done && !any_pending(s)) {
+        const double t = elapsed(&s->t0);
+        pthread_mutex_lock(&s->mu);
+        s->st.busy_seconds += t - s->busy_since;
+        pthread_mutex_unlock(&s->mu);
+    }
     return done;
 }
 

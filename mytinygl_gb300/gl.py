@@ -137,7 +137,8 @@ class ServerStats(ctypes.Structure):
     """mtgl_server_stats (include/mytinygl/mtgl_serve.h)"""
     _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "failed", "batches",
                                                "deferred_for_budget", "peak_bytes_admitted",
-                                               "framebuffers_allocated")] + [("busy_seconds", ctypes.c_double)]
+                                               "framebuffers_allocated")] + [("busy_seconds", ctypes.c_double),
+                                                                             ("kernel_launches", ctypes.c_uint64)]
 
 
 class GLLibrary:

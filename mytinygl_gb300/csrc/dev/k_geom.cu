@@ -397,9 +397,15 @@ __device__ __forceinline__ uint32_t depth_rejection(const DevRaster &R, float z0
     if (rs.depth_func == GL_NEVER) return ZC_NEVER;
     if (rs.depth_func != GL_LESS && rs.depth_func != GL_LEQUAL) return ZC_NONE;
     if (!isfinite(z0) || !isfinite(z1) || !isfinite(z2)) return ZC_NONE;
-    const double sx = (double)fmaxf(fmaxf(fx0, fx1), fx2) - (double)fminf(fminf(fx0, fx1), fx2);
-    const double sy = (double)fmaxf(fmaxf(fy0, fy1), fy2) - (double)fminf(fminf(fy0, fy1), fy2);
-    if (!(sx * sy < 8388608.0)) return ZC_NONE;
+    // The spans are differences of integer-valued floats, exact in float below 2^24; their
+    // product is taken exactly in 64-bit integers (no FP64: this GPU's FP64 pipe is narrow).
+    const float sx = fmaxf(fmaxf(fx0, fx1), fx2) - fminf(fminf(fx0, fx1), fx2);
+    const float sy = fmaxf(fmaxf(fy0, fy1), fy2) - fminf(fminf(fy0, fy1), fy2);
+    bool small;
+    if (sx == 0.0f || sy == 0.0f) small = true;
+    else if (sx < 0x1p23f && sy < 0x1p23f) small = (uint64_t)small_trunc(sx) * (uint64_t)small_trunc(sy) < (1ull << 23);
+    else small = false;
+    if (!small) return ZC_NONE;
     return rs.depth_func == GL_LESS ? ZC_LESS : ZC_LEQUAL;
 }
 

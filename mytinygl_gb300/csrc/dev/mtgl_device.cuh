@@ -146,31 +146,49 @@ __device__ __forceinline__ int32_t x86_f2i(float f)
     return (f >= -2147483648.0f && f < 2147483648.0f) ? (int32_t)f : INT32_MIN;
 }
 
+// Exact small conversions on the FP32 adder instead of the conversion unit, which issues at
+// a fraction of the FP32 rate. For 0 <= v < 2^23 the float with bits 0x4B000000 | v is
+// 2^23 + v; for a float f, 2^23 + f (or 1.5 * 2^23 + f) lies in [2^23, 2^24), where floats
+// are the integers, so the sum rounded toward zero (or down) is 2^23 + the integer part of
+// f (or 1.5 * 2^23 + floor f), read back from the low mantissa bits.
+// (float)v for 0 <= v < 2^23
+__device__ __forceinline__ float small_u2f(uint32_t v) { return __int_as_float(0x4B000000 | v) - 0x1p23f; }
+// (int32_t)f, truncating, for 0 <= f < 2^23
+__device__ __forceinline__ int32_t small_trunc(float f) { return __float_as_int(__fadd_rz(f, 0x1p23f)) - 0x4B000000; }
+// (int32_t)floorf(f), with floorf(f) in *fl, for -2^22 <= f < 2^22
+__device__ __forceinline__ int32_t small_floor(float f, float *fl)
+{
+    const float s = __fadd_rd(f, 0x1.8p23f);
+    *fl = s - 0x1.8p23f;
+    return __float_as_int(s) - 0x4B400000;
+}
+
 // (float)v / 255.0f (graphics.h:350-357, textures.c:294-307) for v in [0, 255], without a
 // division: the product with the rounded reciprocal, corrected once by its exact residual
 // (Markstein's FMA correction). The result equals the IEEE quotient for every byte value
 // (checked exhaustively with exact rational arithmetic in tests/test_arith.py).
 __device__ __forceinline__ float u8f(uint32_t v)
 {
-    const float x = (float)v;
+    const float x = small_u2f(v);
     const float r = 0x1.010102p-8f;  // 1.0f / 255.0f rounded to float
     const float q = x * r;
     const float e = __fmaf_rn(-q, 255.0f, x);
     return __fmaf_rn(e, r, q);
 }
 
+// one channel of color_to_rgba32: the reference clamps with two compares, which pass a
+// NaN through to a conversion giving INT32_MIN, whose low byte is 0; fmaxf / fminf map a NaN
+// to 0 first, and every other input to the same clamped value (a -0 may come out as +0,
+// which truncates to the same byte)
+__device__ __forceinline__ uint32_t pack_channel(float c)
+{
+    return (uint32_t)small_trunc(fminf(fmaxf(c, 0.0f), 1.0f) * 255.0f) & 0xFFu;
+}
+
 // color_to_rgba32 (graphics.h:337-348)
 __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a)
 {
-    float rf = r < 0.0f ? 0.0f : (r > 1.0f ? 1.0f : r);
-    float gf = g < 0.0f ? 0.0f : (g > 1.0f ? 1.0f : g);
-    float bf = b < 0.0f ? 0.0f : (b > 1.0f ? 1.0f : b);
-    float af = a < 0.0f ? 0.0f : (a > 1.0f ? 1.0f : a);
-    uint32_t ri = (uint32_t)x86_f2i(rf * 255.0f) & 0xFFu;
-    uint32_t gi = (uint32_t)x86_f2i(gf * 255.0f) & 0xFFu;
-    uint32_t bi = (uint32_t)x86_f2i(bf * 255.0f) & 0xFFu;
-    uint32_t ai = (uint32_t)x86_f2i(af * 255.0f) & 0xFFu;
-    return (ai << 24) | (bi << 16) | (gi << 8) | ri;
+    return (pack_channel(a) << 24) | (pack_channel(b) << 16) | (pack_channel(g) << 8) | pack_channel(r);
 }
 
 __device__ __forceinline__ float4 unpack_rgba(uint32_t p)
@@ -329,8 +347,20 @@ __device__ __forceinline__ uint32_t sample_level(const TexView &t, int32_t ws, i
     float tx = u * (float)t.w - 0.5f;
     float ty = v * (float)t.h - 0.5f;
     if (linear) {
-        int32_t x0 = x86_f2i(floorf(tx)), y0 = x86_f2i(floorf(ty));
-        float fx = tx - (float)x0, fy = ty - (float)y0;
+        int32_t x0, y0;
+        float fx, fy;
+        if (fabsf(tx) < 0x1p22f && fabsf(ty) < 0x1p22f) {  // every in-range coordinate
+            float flx, fly;
+            x0 = small_floor(tx, &flx);
+            y0 = small_floor(ty, &fly);
+            fx = tx - flx;
+            fy = ty - fly;
+        } else {
+            x0 = x86_f2i(floorf(tx));
+            y0 = x86_f2i(floorf(ty));
+            fx = tx - (float)x0;
+            fy = ty - (float)y0;
+        }
         const bool rs = ws == GL_REPEAT, rt = wt == GL_REPEAT;
         const int32_t xa = wrap_coord(x0, t.w, rs), xb = wrap_next(xa, x0, t.w, rs);
         const int32_t ya = wrap_coord(y0, t.h, rt), yb = wrap_next(ya, y0, t.h, rt);
@@ -343,7 +373,16 @@ __device__ __forceinline__ uint32_t sample_level(const TexView &t, int32_t ws, i
         float4 r = lerp_col(top, bot, fy);
         return pack_rgba(r.x, r.y, r.z, r.w);
     }
-    int32_t x = x86_f2i(floorf(tx + 0.5f)), y = x86_f2i(floorf(ty + 0.5f));
+    const float hx = tx + 0.5f, hy = ty + 0.5f;
+    int32_t x, y;
+    float fl;
+    if (fabsf(hx) < 0x1p22f && fabsf(hy) < 0x1p22f) {
+        x = small_floor(hx, &fl);
+        y = small_floor(hy, &fl);
+    } else {
+        x = x86_f2i(floorf(hx));
+        y = x86_f2i(floorf(hy));
+    }
     if (x < 0) x = 0;
     if (x >= t.w) x = t.w - 1;
     if (y < 0) y = 0;
@@ -359,18 +398,27 @@ __device__ __forceinline__ uint32_t sample_mip1(const DevRaster &R, float u, flo
     return sample_level(m, R.rs.tex_wrap_s, R.rs.tex_wrap_t, u, v, lin);
 }
 
+// (float)x86_f2i(f): the truncated value as a float (INT32_MIN outside the int range)
+__device__ __forceinline__ float trunc_f2i_f(float f)
+{
+    const float a = fabsf(f);
+    if (!(a < 0x1p22f)) return (float)x86_f2i(f);
+    const float t = __fadd_rz(a, 0x1p23f) - 0x1p23f;  // trunc |f|: +0 for |f| < 1, as (float)0 is
+    return f < 0.0f ? -t : t;  // a -0 here only meets u - t, where it acts as +0
+}
+
 __device__ inline uint32_t sample_lod(const DevRaster &R, float u, float v, float lod)
 {
     const int32_t ws = R.rs.tex_wrap_s, wt = R.rs.tex_wrap_t;
     if (ws == GL_REPEAT) {
-        u = u - (float)x86_f2i(u);
+        u = u - trunc_f2i_f(u);
         if (u < 0) u += 1.0f;
     } else {
         if (u < 0.0f) u = 0.0f;
         if (u > 1.0f) u = 1.0f;
     }
     if (wt == GL_REPEAT) {
-        v = v - (float)x86_f2i(v);
+        v = v - trunc_f2i_f(v);
         if (v < 0) v += 1.0f;
     } else {
         if (v < 0.0f) v = 0.0f;
@@ -482,12 +530,20 @@ __device__ __forceinline__ float fog_factor(const mtgl_raster_state &rs, float f
     return f;
 }
 
+// the double-precision depth range map, out of line: inlined, its few FP64 instructions
+// are issued (predicated off) for every fragment of the default range as well, and the
+// FP64 pipe of this GPU is narrow
+static __device__ __noinline__ float map_depth_range(float t, double near_d, double far_d)
+{
+    return (float)((double)t * (far_d - near_d) + near_d);
+}
+
 // depth range mapping (raster.c:548): float NDC term, double range, float result
 __device__ __forceinline__ float map_depth(const DevRaster &R, float z)
 {
     float t = (z + 1.0f) * 0.5f;
     if (R.default_depth_range) return t;  // (double)t * 1.0 + 0.0 rounds back to t
-    return (float)((double)t * (R.rs.depth_far - R.rs.depth_near) + R.rs.depth_near);
+    return map_depth_range(t, R.rs.depth_near, R.rs.depth_far);
 }
 
 // write_pixel_masked (raster.c:20-45) on a packed destination pixel

@@ -511,6 +511,76 @@ def sc_list_blocks():
     return s
 
 
+def _limit_frame(name, w, h, tex_w, tex_h):
+    """A framebuffer at the reference's largest side (16384, framebuffer.h:30) with a texture
+    at its largest side (2048, textures.h:17): long thin triangles, lines and points across
+    the whole frame, flat and textured, depth tested."""
+    s = base(name, w, h, persp=False)
+    rng = np.random.default_rng(w * 7 + h)
+    checker_texture(s, size=(tex_w, tex_h), seed=13)
+    s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MIN_FILTER, G.GL_LINEAR_MIPMAP_LINEAR)
+    s.glEnable(G.GL_DEPTH_TEST)
+    for textured in (False, True):
+        (s.glEnable if textured else s.glDisable)(G.GL_TEXTURE_2D)
+        s.glBegin(G.GL_TRIANGLES)
+        for _ in range(12):
+            c = rng.uniform(0, 1, 4)
+            s.glColor4f(*map(float, c))
+            s.glTexCoord2f(*map(float, rng.uniform(-0.5, 1.5, 2)))
+            s.glVertex3f(*map(float, rng.uniform(-1.1, 1.1, 3)))
+        s.glEnd()
+    s.glDisable(G.GL_TEXTURE_2D)
+    s.glLineWidth(2.0)
+    _block(s, rng, G.GL_LINE_STRIP, 6, normal=None, spread=1.0, z=(-0.9, 0.9))
+    s.glPointSize(3.0)
+    _block(s, rng, G.GL_POINTS, 10, normal=None, spread=1.0, z=(-0.9, 0.9))
+    return s
+
+
+def sc_max_width():
+    return _limit_frame("max_width", 16384, 8, 2048, 4)
+
+
+def sc_max_height():
+    return _limit_frame("max_height", 8, 16384, 4, 2048)
+
+
+def sc_ragged():
+    """Empty and ragged inputs: every mode with 0-5 vertices (incomplete primitives dropped),
+    empty glBegin/glEnd, zero-count and negative-first array draws, a zero-size viewport,
+    degenerate triangles, and a texture one texel over the size limit (refused)."""
+    s = base("ragged")
+    rng = np.random.default_rng(47)
+    s.glEnable(G.GL_DEPTH_TEST)
+    s.glTranslatef(0.0, 0.0, -4.0)
+    for mode in (G.GL_POINTS, G.GL_LINES, G.GL_LINE_LOOP, G.GL_LINE_STRIP, G.GL_TRIANGLES, G.GL_TRIANGLE_STRIP,
+                 G.GL_TRIANGLE_FAN, G.GL_QUADS, G.GL_QUAD_STRIP, G.GL_POLYGON):
+        for n in range(6):
+            _block(s, rng, mode, n, normal=None, spread=2.0, z=(-1.0, 1.0))
+    s.glBegin(G.GL_TRIANGLES)  # degenerate: a repeated vertex, then three collinear ones
+    for p in ((0.1, 0.1, 0.0), (0.1, 0.1, 0.0), (0.9, 0.5, 0.0), (-1.0, -1.0, 0.0), (0.0, 0.0, 0.0),
+              (1.0, 1.0, 0.0)):
+        s.glVertex3f(*p)
+    s.glEnd()
+    pos = rng.uniform(-2, 2, (12, 3)).astype(np.float32)
+    s.glEnableClientState(G.GL_VERTEX_ARRAY)
+    s.glVertexPointer(3, G.GL_FLOAT, 0, pos)
+    s.glDrawArrays(G.GL_TRIANGLES, 0, 0)
+    s.glDrawArrays(G.GL_TRIANGLES, -2, 8)  # elements before the array read the defaults
+    s.glDrawElements(G.GL_TRIANGLES, 0, G.GL_UNSIGNED_SHORT, np.zeros(3, np.uint16))
+    s.glDisableClientState(G.GL_VERTEX_ARRAY)
+    s.glViewport(10, 10, 0, 0)
+    _block(s, rng, G.GL_TRIANGLES, 6, normal=None, spread=2.0, z=(-1.0, 1.0))
+    s.glViewport(0, 0, W, H)
+    big = np.zeros((2, 2049, 4), np.uint8)
+    s.glGenTextures(1, np.zeros(1, np.uint32))
+    s.glBindTexture(G.GL_TEXTURE_2D, 1)
+    s.glTexImage2D(G.GL_TEXTURE_2D, 0, G.GL_RGBA, 2049, 2, 0, G.GL_RGBA, G.GL_UNSIGNED_BYTE, big)
+    s.glEnable(G.GL_TEXTURE_2D)
+    _block(s, rng, G.GL_TRIANGLES, 6, uv=True, normal=None, spread=2.0, z=(-1.0, 1.0))
+    return s
+
+
 def sc_vertex_arrays():
     s = base("vertex_arrays")
     rng = np.random.default_rng(30)
@@ -843,6 +913,9 @@ SCENES = {
     "viewport": (sc_viewport, ()),
     "display_lists": (sc_display_lists, ()),
     "list_blocks": (sc_list_blocks, ()),
+    "max_width": (sc_max_width, ("lines",)),
+    "max_height": (sc_max_height, ("lines",)),
+    "ragged": (sc_ragged, ("lines",)),
     "vertex_arrays": (sc_vertex_arrays, ()),
     "vbo": (sc_vbo, ()),
     "state_in_begin_end": (sc_state_in_begin_end, ()),

@@ -240,3 +240,11 @@ def test_list_block_device_resident(gpu, oracle, late):
         ctx.destroy()
     stats = harness.compare(out[0] + (0,), out[1] + (0,))
     harness.assert_parity(stats, color_tol=1, name="list_block")
+
+
+def test_context_size_limits(gpu):
+    """The same framebuffer size limits as the reference (framebuffer.h:30-35)."""
+    import test_oracle
+
+    for (w, h), ok in test_oracle.SIZE_CASES:
+        assert test_oracle.context_created(gpu, w, h) == ok, (w, h)

@@ -75,3 +75,25 @@ def test_oracle_matches_reference_headline(oracle, ref, which):
     }[which]()
     stats = harness.compare(render(ref, scene), render(oracle, scene), harness.cleared_buffers(scene))
     harness.assert_parity(stats, color_tol=0, name=which)
+
+
+SIZE_CASES = [((16384, 1), True), ((1, 16384), True), ((16385, 1), False), ((1, 16385), False), ((0, 4), False),
+              ((4, 0), False), ((-1, 4), False)]
+
+
+def context_created(lib, w, h):
+    h_ = lib.lib.gl_create_context(w, h)
+    if h_:
+        lib.lib.gl_destroy_context(h_)
+    return bool(h_)
+
+
+def test_context_size_limits(oracle):
+    """Framebuffer sides are 1..16384 (framebuffer.h:30-35): larger or empty ones are refused."""
+    for (w, h), ok in SIZE_CASES:
+        assert context_created(oracle, w, h) == ok, (w, h)
+
+
+def test_context_size_limits_match_reference(ref):
+    for (w, h), ok in SIZE_CASES:
+        assert context_created(ref, w, h) == ok, (w, h)

@@ -430,6 +430,10 @@ __device__ inline uint32_t sample_lod(const DevRaster &R, float u, float v, floa
         if (lod >= 0.5f) return sample_mip1(R, u, v, filter);
         filter = (filter == GL_NEAREST_MIPMAP_NEAREST) ? GL_NEAREST : GL_LINEAR;
     } else if (filter == GL_NEAREST_MIPMAP_LINEAR || filter == GL_LINEAR_MIPMAP_LINEAR) {
+        // From lod 1 up the weight of level 1 is 1: lerp_col(c0, c1, 1) gives c1's channels
+        // exactly (c0 * 0 + c1 * 1), and packing them gives c1 back (truncating
+        // ((float)b / 255) * 255 returns b for every byte), so level 0 is not sampled.
+        if (lod >= 1.0f) return sample_mip1(R, u, v, filter);
         if (lod > 0.0f) {
             float cl = (lod > 1.0f) ? 1.0f : lod;
             uint32_t c0 = sample_level(base, ws, wt, u, v, filter == GL_LINEAR_MIPMAP_LINEAR);

@@ -103,3 +103,37 @@ def test_line_step_closed_form_matches_the_loop():
                 else:
                     want = (3, -5)
                 assert (cx, cy) == want, (dx, dy, k)
+
+
+def test_mip_blend_at_weight_one_returns_level_one():
+    """sample_lod skips level 0 from lod 1 up: lerp_col(c0, c1, 1) = c0 * 0 + c1 * 1 is c1's
+    channel value exactly, and packing a channel value back gives the byte: trunc(round(
+    round(b / 255) * 255)) == b for every byte, computed here with exact rationals rounded
+    to float32 at each step (the same steps as unpack_rgba / pack_rgba)."""
+    for b in range(256):
+        u = round_f32(Fr(b, 255))
+        assert u * 0 + u * 1 == u
+        back = round_f32(u * 255)
+        assert back.numerator // back.denominator == b, b
+
+
+def test_small_conversions_by_directed_rounding():
+    """small_trunc / small_floor / small_u2f: adding 2^23 (1.5 * 2^23) rounded toward zero
+    (down) leaves the integer part in the low mantissa bits. Checked on the boundaries and
+    on random values with exact rationals, rounding as the GPU's fadd.rz / fadd.rm do."""
+    def add_directed(a: Fr, b: Fr, mode: str) -> Fr:
+        s = a + b  # positive, in [2^23, 2^24): float32 spacing is 1, so both modes floor
+        assert mode in ("rz", "rd") and 2 ** 23 <= s < 2 ** 24
+        return Fr(s.numerator // s.denominator)
+    rng = np.random.default_rng(3)
+    vals = [0.0, 0.5, 1.0, 254.999, 255.0, 2.0 ** 22 - 0.5] + list(rng.uniform(0, 2 ** 22, 200))
+    for v in vals:
+        f = Fr(float(np.float32(v)))
+        t = add_directed(f, Fr(2 ** 23), "rz") - 2 ** 23
+        assert t == int(float(f)), v
+    for v in [-2.0 ** 22, -1.5, -1.0, -0.5, -1e-7, 0.0, 0.25, 7.75] + list(rng.uniform(-2 ** 22, 2 ** 22, 200)):
+        f = Fr(float(np.float32(v)))
+        s = add_directed(f, Fr(3 * 2 ** 22), "rd")
+        assert s - 3 * 2 ** 22 == np.floor(float(f)), v
+    for v in (0, 1, 255, 2 ** 23 - 1):
+        assert np.array([0x4B000000 | v], np.uint32).view(np.float32)[0] - np.float32(2 ** 23) == v

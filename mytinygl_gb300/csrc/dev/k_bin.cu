@@ -309,20 +309,26 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const uint32_t *ke
 
 // Stable scatter: warp w owns items [w*256, w*256+256) of the block, taken 32 at a time in
 // order; match-any groups equal digits, the leader advances the warp's digit counter, and
-// per-digit prefix sums over warps and blocks place every item after all earlier ones.
+// per-digit prefix sums over warps and blocks place every item after all earlier ones. The
+// block first sorts its items by digit in shared memory, so that each digit's run leaves
+// as consecutive addresses (coalesced writes) rather than one scattered word per item.
 __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t *keys, const uint32_t *vals,
                                                                 uint32_t cap, const uint32_t *n_dev, int shift,
                                                                 uint32_t mask,
                                                                 const uint32_t *hist_scan, uint32_t nblocks,
                                                                 uint32_t *keys_out, uint32_t *vals_out)
 {
-    __shared__ uint32_t wcount[kRadixWarps][kRadixDigits];
+    __shared__ uint32_t wcount[kRadixWarps][kRadixDigits];  // per warp and digit: count, then block-local start
+    __shared__ uint32_t dstart[kRadixDigits];                // block-local start of each digit's run
+    __shared__ uint32_t gdelta[kRadixDigits];                // global start minus block-local start
+    __shared__ uint32_t skey[kRadixTile], sval[kRadixTile];
     const uint32_t n = min(*n_dev, cap);
     const int ndig = (int)mask + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kRadixWarps * kRadixDigits; i += kRadixThreads) (&wcount[0][0])[i] = 0;
     __syncthreads();
-    const uint32_t wbase = blockIdx.x * (uint32_t)kRadixTile + warp * 32 * kRadixItems;
+    const uint32_t bbase = blockIdx.x * (uint32_t)kRadixTile;
+    const uint32_t wbase = bbase + warp * 32 * kRadixItems;
     const uint32_t lt = (1u << lane) - 1u;
     uint32_t key[kRadixItems], val[kRadixItems], rank[kRadixItems];
 #pragma unroll
@@ -341,24 +347,63 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_scatter(const uint32_t 
         rank[k] = pre + __popc(peers & lt);
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < ndig; d += kRadixThreads) {
-        uint32_t run = hist_scan[(size_t)d * nblocks + blockIdx.x];
+    // per digit: the block's count, then each warp's start within the digit's run
+    for (int d = threadIdx.x; d < kRadixDigits; d += kRadixThreads) {
+        uint32_t run = 0;
 #pragma unroll
         for (int w = 0; w < kRadixWarps; w++) {
-            const uint32_t c = wcount[w][d];
+            const uint32_t c = d < ndig ? wcount[w][d] : 0u;
             wcount[w][d] = run;
             run += c;
         }
+        dstart[d] = run;  // the count for now
     }
     __syncthreads();
+    // exclusive scan of the digit counts (512 entries, 2 per thread) into block-local starts
+    {
+        const int d0 = 2 * threadIdx.x;
+        const uint32_t c0 = dstart[d0], c1 = dstart[d0 + 1];
+        uint32_t incl = c0 + c1, x = incl;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        __shared__ uint32_t wsum[kRadixWarps];
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        uint32_t before = 0;
+        for (int w = 0; w < warp; w++) before += wsum[w];
+        const uint32_t excl = before + x - incl;
+        __syncthreads();
+        dstart[d0] = excl;
+        dstart[d0 + 1] = excl + c0;
+        if (d0 < ndig) gdelta[d0] = hist_scan[(size_t)d0 * nblocks + blockIdx.x] - excl;
+        if (d0 + 1 < ndig) gdelta[d0 + 1] = hist_scan[(size_t)(d0 + 1) * nblocks + blockIdx.x] - (excl + c0);
+    }
+    __syncthreads();
+    // items into shared memory in digit order (stable: warp order, then item order)
 #pragma unroll
     for (int k = 0; k < kRadixItems; k++) {
         const uint32_t i = wbase + k * 32 + lane;
         if (i < n) {
             const uint32_t d = (key[k] >> shift) & mask;
-            const uint32_t pos = wcount[warp][d] + rank[k];
-            keys_out[pos] = key[k];
-            vals_out[pos] = val[k];
+            const uint32_t at = dstart[d] + wcount[warp][d] + rank[k];
+            skey[at] = key[k];
+            sval[at] = val[k];
+        }
+    }
+    __syncthreads();
+    // consecutive slots of one digit go to consecutive global positions
+    const uint32_t valid_n = n > bbase ? min((uint32_t)kRadixTile, n - bbase) : 0u;
+#pragma unroll
+    for (int k = 0; k < kRadixItems; k++) {
+        const uint32_t at = k * kRadixThreads + threadIdx.x;
+        if (at < valid_n) {
+            const uint32_t kk = skey[at];
+            const uint32_t pos = gdelta[(kk >> shift) & mask] + at;
+            keys_out[pos] = kk;
+            vals_out[pos] = sval[at];
         }
     }
 }

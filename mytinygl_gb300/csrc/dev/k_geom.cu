@@ -249,6 +249,67 @@ __device__ __forceinline__ int clip_start(const float4 &a, const float4 &b, cons
     return kClipNone;
 }
 
+// The Sutherland-Hodgman pass of plane p over a triangle, in registers, for the common case
+// of a triangle crossing one plane. Writes the pass's output polygon (3 or 4 vertices, in the
+// pass's order) and returns its size; returns 0 when the general clipper must run instead:
+// an intersection the pass drops (|den| <= 1e-10), or an output vertex not inside a later
+// plane (a later pass would change the polygon; a pass whose vertices are all inside copies
+// them unchanged, in order).
+template <class V>
+__device__ __forceinline__ int clip_one_plane(const V &v0, const V &v1, const V &v2, int p, V &o0, V &o1, V &o2,
+                                              V &o3)
+{
+    const float d0 = plane_dist(v0.clip, p), d1 = plane_dist(v1.clip, p), d2 = plane_dist(v2.clip, p);
+    const bool i0 = d0 >= 0.0f, i1 = d1 >= 0.0f, i2 = d2 >= 0.0f;
+    // the intersection the pass puts on edge a -> b
+    auto cross = [p](const V &a, const V &b, float da, float db, V &out) -> bool {
+        const float den = da - db;
+        if (!(fabsf(den) > 1e-10f)) return false;
+        out = cv_lerp(a, b, da / den);
+        snap_plane(out, p);
+        return true;
+    };
+    bool ok;
+    int n;
+    if (i0 && !i1 && !i2) {         // edges 2->0, 0->1 cross: X20 v0 X01
+        ok = cross(v2, v0, d2, d0, o0) && cross(v0, v1, d0, d1, o2);
+        o1 = v0;
+        n = 3;
+    } else if (!i0 && i1 && !i2) {  // X01 v1 X12
+        ok = cross(v0, v1, d0, d1, o0) && cross(v1, v2, d1, d2, o2);
+        o1 = v1;
+        n = 3;
+    } else if (!i0 && !i1 && i2) {  // X20 X12 v2
+        ok = cross(v2, v0, d2, d0, o0) && cross(v1, v2, d1, d2, o1);
+        o2 = v2;
+        n = 3;
+    } else if (i0 && i1 && !i2) {   // X20 v0 v1 X12
+        ok = cross(v2, v0, d2, d0, o0) && cross(v1, v2, d1, d2, o3);
+        o1 = v0;
+        o2 = v1;
+        n = 4;
+    } else if (!i0 && i1 && i2) {   // X20 X01 v1 v2
+        ok = cross(v2, v0, d2, d0, o0) && cross(v0, v1, d0, d1, o1);
+        o2 = v1;
+        o3 = v2;
+        n = 4;
+    } else if (i0 && !i1 && i2) {   // v0 X01 X12 v2
+        ok = cross(v0, v1, d0, d1, o1) && cross(v1, v2, d1, d2, o2);
+        o0 = v0;
+        o3 = v2;
+        n = 4;
+    } else {
+        return 0;
+    }
+    if (!ok) return 0;
+    for (int q = p + 1; q < 6; q++) {
+        if (!(plane_dist(o0.clip, q) >= 0.0f) || !(plane_dist(o1.clip, q) >= 0.0f) ||
+            !(plane_dist(o2.clip, q) >= 0.0f) || (n == 4 && !(plane_dist(o3.clip, q) >= 0.0f)))
+            return 0;
+    }
+    return n;
+}
+
 // clip_triangle (clipping.h:106-126): Sutherland-Hodgman passes from plane `first` on (the
 // earlier ones copy the triangle unchanged, see clip_start); result in bufA[0..n)
 template <class V>
@@ -894,13 +955,25 @@ __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
         const RecOut o = rec_out(A, t, EMIT, EYE);
         uint32_t e0, e1, e2;
         element_triple(D.mode, P.k, e0, e1, e2);
-        V bufA[kClipMax], bufB[kClipMax];
-        load_cv(A, element_slot(D, e0), bufA[0]);
-        load_cv(A, element_slot(D, e1), bufA[1]);
-        load_cv(A, element_slot(D, e2), bufA[2]);
-        const int start = clip_start(bufA[0].clip, bufA[1].clip, bufA[2].clip);
+        V v0, v1, v2;
+        load_cv(A, element_slot(D, e0), v0);
+        load_cv(A, element_slot(D, e1), v1);
+        load_cv(A, element_slot(D, e2), v2);
+        const int start = clip_start(v0.clip, v1.clip, v2.clip);
         uint32_t produced = 0;
-        const int nv = (start < kClipNone) ? clip_triangle(bufA, bufB, start) : 0;
+        V bufA[kClipMax];
+        int nv = 0;
+        if (start < kClipNone) {
+            // one plane crossed: the pass in registers; otherwise the general clipper
+            nv = clip_one_plane(v0, v1, v2, start, bufA[0], bufA[1], bufA[2], bufA[3]);
+            if (!nv) {
+                V bufB[kClipMax];
+                bufA[0] = v0;
+                bufA[1] = v1;
+                bufA[2] = v2;
+                nv = clip_triangle(bufA, bufB, start);
+            }
+        }
         if (nv >= 3) {
             for (int j = 0; j < nv; j++) persp_divide(bufA[j]);
             for (int j = 1; j + 1 < nv; j++)

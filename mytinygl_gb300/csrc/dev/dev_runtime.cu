@@ -43,6 +43,51 @@ int index_size(uint32_t type)
     return type == GL_UNSIGNED_INT ? 4 : (type == GL_UNSIGNED_SHORT ? 2 : 1);
 }
 
+// the tile kernel's packed copy of the fragment stages' state (FragState)
+void pack_frag_state(DevRaster &R)
+{
+    const mtgl_raster_state &rs = R.rs;
+    FragState &f = R.fs;
+    memset(&f, 0, sizeof(f));
+    uint32_t c = 0;
+    if (rs.stencil_test) c |= FC_STENCIL;
+    if (rs.depth_test) c |= FC_DEPTH;
+    if (rs.depth_test && rs.depth_mask) c |= FC_DEPTH_WRITE;
+    if (rs.shade_model == GL_FLAT) c |= FC_FLAT;
+    if (rs.alpha_test) c |= FC_ALPHA;
+    if (rs.perspective_hint == GL_FASTEST) c |= FC_AFFINE_UV;
+    if (rs.fog) c |= FC_FOG;
+    if (rs.blend) c |= FC_BLEND;
+    if (R.default_depth_range) c |= FC_DEFAULT_RANGE;
+    uint32_t mask = 0;
+    for (int i = 0; i < 4; i++)
+        if (rs.color_mask[i]) mask |= 1u << i;
+    if (mask == 15u) c |= FC_MASK_ALL;
+    if (mask == 0u) c |= FC_MASK_NONE;
+    if (R.tex) c |= FC_TEXTURE;
+    f.ctl = c;
+    f.depth_func = rs.depth_func;
+    f.alpha_func = rs.alpha_func;
+    f.tex_env_mode = rs.tex_env_mode;
+    f.stencil_func = rs.stencil_func;
+    f.stencil_ref = rs.stencil_ref;
+    f.stencil_mask = rs.stencil_mask;
+    f.stencil_writemask = rs.stencil_writemask;
+    f.stencil_fail = rs.stencil_fail;
+    f.stencil_zfail = rs.stencil_zfail;
+    f.stencil_zpass = rs.stencil_zpass;
+    f.alpha_ref = rs.alpha_ref;
+    f.blend_src = rs.blend_src;
+    f.blend_dst = rs.blend_dst;
+    f.fog_mode = rs.fog_mode;
+    f.fog_density = rs.fog_density;
+    f.fog_start = rs.fog_start;
+    f.fog_end = rs.fog_end;
+    f.color_mask = mask;
+    memcpy(f.fog_color, rs.fog_color, sizeof(f.fog_color));
+    memcpy(f.tex_env_color, rs.tex_env_color, sizeof(f.tex_env_color));
+}
+
 uint32_t push_raster(mtgl_dev *d, const mtgl_raster_state *rs)
 {
     Pass &P = d->pass;
@@ -63,6 +108,7 @@ uint32_t push_raster(mtgl_dev *d, const mtgl_raster_state *rs)
     R.default_depth_range = (rs->depth_near == 0.0 && rs->depth_far == 1.0) ? 1 : 0;
     R.needs_eye = (rs->lighting && (rs->shade_model == GL_PHONG || rs->lit.two_side)) ? 1 : 0;
     R.depth_rejection = d->depth_rejection ? 1 : 0;
+    pack_frag_state(R);
     if (R.needs_eye) P.needs_eye = true;
     P.raster_src.push_back(*rs);
     P.rasters.push_back(R);

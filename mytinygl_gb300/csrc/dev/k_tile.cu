@@ -73,55 +73,65 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__re
     const float4 q3 = __ldg(r4 + 3);    // Z0 Z1 Z2 DMIN
     const float4 q11 = __ldg(r4 + 11);  // EZ0 EZ1 EZ2 RASTER
     const DevRaster &R = A.rasters[min(__float_as_uint(q11.w), A.nrasters - 1)];
-    const mtgl_raster_state &rs = R.rs;
+    // the fragment stages' packed state: the enables word, then each stage's operands as the
+    // stage needs them (loaded where used, from one cached line, to keep few registers live)
+    const FragState &S = R.fs;
+    const uint32_t ctl = __ldg(&S.ctl);
     const float z = b0 * q3.x + b1 * q3.y + b2 * q3.z;
-    const float depth = map_depth(R, z);
+    const float t = (z + 1.0f) * 0.5f;
+    const float depth = (ctl & FC_DEFAULT_RANGE) ? t : map_depth_range(t, R.rs.depth_near, R.rs.depth_far);
 
     uint32_t sv = 0;
-    if (rs.stencil_test) {
+    if (ctl & FC_STENCIL) {
+        const uint4 g = __ldg(reinterpret_cast<const uint4 *>(&S) + 1);  // func, ref, mask, writemask
         sv = st;
-        if (!stencil_pass(rs.stencil_func, rs.stencil_ref, rs.stencil_mask, sv)) {
-            st = stencil_write(st, stencil_apply(rs.stencil_fail, sv, rs.stencil_ref), rs.stencil_writemask);
+        if (!stencil_pass(g.x, (int32_t)g.y, g.z, sv)) {
+            st = stencil_write(st, stencil_apply(__ldg(&S.stencil_fail), sv, (int32_t)g.y), g.w);
             return false;
         }
     }
-    if (rs.depth_test && !cmp_pass(rs.depth_func, depth, dep)) {
-        if (rs.stencil_test)
-            st = stencil_write(st, stencil_apply(rs.stencil_zfail, sv, rs.stencil_ref), rs.stencil_writemask);
+    if ((ctl & FC_DEPTH) && !cmp_pass(__ldg(&S.depth_func), depth, dep)) {
+        if (ctl & FC_STENCIL)
+            st = stencil_write(st, stencil_apply(__ldg(&S.stencil_zfail), sv, __ldg(&S.stencil_ref)),
+                               __ldg(&S.stencil_writemask));
         return false;
     }
-    if (rs.stencil_test)
-        st = stencil_write(st, stencil_apply(rs.stencil_zpass, sv, rs.stencil_ref), rs.stencil_writemask);
+    if (ctl & FC_STENCIL)
+        st = stencil_write(st, stencil_apply(__ldg(&S.stencil_zpass), sv, __ldg(&S.stencil_ref)),
+                           __ldg(&S.stencil_writemask));
 
     float4 c;
     const float4 c2 = __ldg(r4 + 7);  // C2
-    if (rs.shade_model == GL_FLAT) {
+    if (ctl & FC_FLAT) {
         c = c2;
     } else {
         const float4 c0 = __ldg(r4 + 5), c1 = __ldg(r4 + 6);  // C0, C1
         c = make_float4(c0.x * b0 + c1.x * b1 + c2.x * b2, c0.y * b0 + c1.y * b1 + c2.y * b2,
                         c0.z * b0 + c1.z * b1 + c2.z * b2, c0.w * b0 + c1.w * b1 + c2.w * b2);
     }
-    if (EYE && rs.lighting && have_eye) {
-        const bool back = (__float_as_uint(q12.x) & 1u) != 0;
-        const bool phong = rs.shade_model == GL_PHONG;
-        if (phong || (back && rs.lit.two_side)) {
-            float3 ep = make_float3(e[0] * b0 + e[6] * b1 + e[12] * b2, e[1] * b0 + e[7] * b1 + e[13] * b2,
-                                    e[2] * b0 + e[8] * b1 + e[14] * b2);
-            float3 en = make_float3(e[3] * b0 + e[9] * b1 + e[15] * b2, e[4] * b0 + e[10] * b1 + e[16] * b2,
-                                    e[5] * b0 + e[11] * b1 + e[17] * b2);
-            const mtgl_material *mat = &rs.lit.front;
-            if (back && rs.lit.two_side) {
-                en = make_float3(en.x * -1.0f, en.y * -1.0f, en.z * -1.0f);
-                mat = &rs.lit.back;
+    if (EYE && have_eye) {
+        const mtgl_raster_state &rs = R.rs;
+        if (rs.lighting) {
+            const bool back = (__float_as_uint(q12.x) & 1u) != 0;
+            const bool phong = rs.shade_model == GL_PHONG;
+            if (phong || (back && rs.lit.two_side)) {
+                float3 ep = make_float3(e[0] * b0 + e[6] * b1 + e[12] * b2, e[1] * b0 + e[7] * b1 + e[13] * b2,
+                                        e[2] * b0 + e[8] * b1 + e[14] * b2);
+                float3 en = make_float3(e[3] * b0 + e[9] * b1 + e[15] * b2, e[4] * b0 + e[10] * b1 + e[16] * b2,
+                                        e[5] * b0 + e[11] * b1 + e[17] * b2);
+                const mtgl_material *mat = &rs.lit.front;
+                if (back && rs.lit.two_side) {
+                    en = make_float3(en.x * -1.0f, en.y * -1.0f, en.z * -1.0f);
+                    mat = &rs.lit.back;
+                }
+                c = compute_lighting(rs.lit, ep, en, *mat);
             }
-            c = compute_lighting(rs.lit, ep, en, *mat);
         }
     }
-    if (TEX && R.tex) {
+    if (TEX && (ctl & FC_TEXTURE)) {
         float u, v;
         const float4 q4 = __ldg(r4 + 4);  // W0 W1 W2 LOD
-        if (rs.perspective_hint != GL_FASTEST) {
+        if (!(ctl & FC_AFFINE_UV)) {
             const float4 q9 = __ldg(r4 + 9), q10 = __ldg(r4 + 10);  // UV2 UW0 VW0 | UW1 VW1 UW2 VW2
             const float uow = b0 * q9.z + b1 * q10.x + b2 * q10.z;
             const float vow = b0 * q9.w + b1 * q10.y + b2 * q10.w;
@@ -136,31 +146,36 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__re
         }
         const float4 tc = unpack_rgba(sample_lod(R, u, v, q4.w));
         // the alpha test applies to textured fragments only (raster.c:639-643)
-        if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) return false;
-        switch (rs.tex_env_mode) {
+        if ((ctl & FC_ALPHA) && !cmp_pass(__ldg(&S.alpha_func), tc.w, __ldg(&S.alpha_ref))) return false;
+        switch (__ldg(&S.tex_env_mode)) {
         case GL_REPLACE: c = tc; break;
         case GL_DECAL: c = lerp_rgb(c, tc, tc.w); break;
-        case GL_BLEND:
-            c = make_float4(c.x * (1.0f - tc.x) + rs.tex_env_color[0] * tc.x,
-                            c.y * (1.0f - tc.y) + rs.tex_env_color[1] * tc.y,
-                            c.z * (1.0f - tc.z) + rs.tex_env_color[2] * tc.z, c.w * tc.w);
+        case GL_BLEND: {
+            const float4 ec = __ldg(reinterpret_cast<const float4 *>(S.tex_env_color));
+            c = make_float4(c.x * (1.0f - tc.x) + ec.x * tc.x, c.y * (1.0f - tc.y) + ec.y * tc.y,
+                            c.z * (1.0f - tc.z) + ec.z * tc.z, c.w * tc.w);
             break;
+        }
         case GL_ADD: c = make_float4(c.x + tc.x, c.y + tc.y, c.z + tc.z, c.w * tc.w); break;
         default: c = make_float4(c.x * tc.x, c.y * tc.y, c.z * tc.z, c.w * tc.w); break;
         }
     }
-    if (rs.fog) {
+    if (ctl & FC_FOG) {
+        const float4 g3 = __ldg(reinterpret_cast<const float4 *>(&S) + 3);  // .z mode, .w density
+        const float4 g4 = __ldg(reinterpret_cast<const float4 *>(&S) + 4);  // .x start, .y end
+        const float4 fcol = __ldg(reinterpret_cast<const float4 *>(S.fog_color));
         const float fc = b0 * q11.x + b1 * q11.y + b2 * q11.z;
-        c = lerp_rgb(ld4(rs.fog_color), c, fog_factor(rs, fc));
+        c = lerp_rgb(fcol, c, fog_factor(__float_as_uint(g3.z), g3.w, g4.x, g4.y, fc));
     }
     bool wrote = false;
-    if (rs.depth_test && rs.depth_mask) {
+    if (ctl & FC_DEPTH_WRITE) {
         dep = depth;
         wrote = true;
     }
-    if (rs.blend) c = blend(rs, c, unpack_rgba(col));
+    if (ctl & FC_BLEND) c = blend(__ldg(&S.blend_src), __ldg(&S.blend_dst), c, unpack_rgba(col));
     c = clamp4(c);
-    col = masked_write(rs, col, c);
+    if (ctl & FC_MASK_ALL) col = pack_rgba(c.x, c.y, c.z, c.w);
+    else if (!(ctl & FC_MASK_NONE)) col = masked_write(__ldg(&S.color_mask), col, c);
     return wrote;
 }
 

@@ -101,8 +101,42 @@ struct DevDraw {
     uint32_t tri_base, tri_count;
 };
 
+// The fragment stages' part of a raster state, packed for the tile kernel: a word of the
+// stage enables and each stage's operands in 16-byte groups, one 128-byte line in all. The
+// full state spans about a kilobyte (mostly lights and materials) and scatters these fields
+// over several lines; per fragment the kernel now loads the first group, and further groups
+// only for the stages its enables switch on.
+enum FragCtl : uint32_t {
+    FC_STENCIL = 1u << 0, FC_DEPTH = 1u << 1, FC_DEPTH_WRITE = 1u << 2, FC_FLAT = 1u << 3, FC_ALPHA = 1u << 4,
+    FC_AFFINE_UV = 1u << 5, FC_FOG = 1u << 6, FC_BLEND = 1u << 7, FC_DEFAULT_RANGE = 1u << 8,
+    FC_MASK_ALL = 1u << 9, FC_MASK_NONE = 1u << 10, FC_TEXTURE = 1u << 11
+};
+struct __align__(16) FragState {
+    uint32_t ctl, depth_func, alpha_func, tex_env_mode;
+    uint32_t stencil_func;
+    int32_t stencil_ref;
+    uint32_t stencil_mask, stencil_writemask;
+    uint32_t stencil_fail, stencil_zfail, stencil_zpass;
+    float alpha_ref;
+    uint32_t blend_src, blend_dst, fog_mode;
+    float fog_density;
+    float fog_start, fog_end;
+    uint32_t color_mask;  // bit i: channel i written
+    uint32_t pad0;
+    float fog_color[4];
+    float tex_env_color[4];
+    uint32_t pad1[4];
+};
+
+static_assert(sizeof(FragState) == 128 && offsetof(FragState, stencil_func) == 16 &&
+                  offsetof(FragState, stencil_fail) == 32 && offsetof(FragState, blend_src) == 48 &&
+                  offsetof(FragState, fog_start) == 64 && offsetof(FragState, fog_color) == 80 &&
+                  offsetof(FragState, tex_env_color) == 96,
+              "FragState groups are read as 16-byte words");
+
 // Raster state with the bound texture resolved to device pointers.
 struct DevRaster {
+    FragState fs;          // derived from rs and tex when the draw is queued
     mtgl_raster_state rs;
     const uint32_t *tex;   // level 0, or null when texturing is off
     const uint32_t *mip1;  // level 1, or null when the reference cannot build it (w or h < 2)
@@ -469,12 +503,17 @@ __device__ __forceinline__ float4 blend_factor(uint32_t f, float4 s, float4 d)
     }
 }
 
-__device__ __forceinline__ float4 blend(const mtgl_raster_state &rs, float4 s, float4 d)
+__device__ __forceinline__ float4 blend(uint32_t src, uint32_t dst, float4 s, float4 d)
 {
-    float4 sf = blend_factor(rs.blend_src, s, d);
-    float4 df = blend_factor(rs.blend_dst, s, d);
+    float4 sf = blend_factor(src, s, d);
+    float4 df = blend_factor(dst, s, d);
     return clamp4(make_float4(s.x * sf.x + d.x * df.x, s.y * sf.y + d.y * df.y, s.z * sf.z + d.z * df.z,
                               s.w * sf.w + d.w * df.w));
+}
+
+__device__ __forceinline__ float4 blend(const mtgl_raster_state &rs, float4 s, float4 d)
+{
+    return blend(rs.blend_src, rs.blend_dst, s, d);
 }
 
 __device__ __forceinline__ bool stencil_pass(uint32_t func, int32_t ref, uint32_t mask, uint32_t val)
@@ -514,16 +553,16 @@ __device__ __forceinline__ uint32_t stencil_write(uint32_t old, uint32_t nv, uin
     return ((old & ~m8) | (nv & m8)) & 0xFFu;
 }
 
-__device__ __forceinline__ float fog_factor(const mtgl_raster_state &rs, float fog_coord)
+__device__ __forceinline__ float fog_factor(uint32_t mode, float density, float start, float end, float fog_coord)
 {
     float f;
-    switch (rs.fog_mode) {
+    switch (mode) {
     case GL_LINEAR:
-        f = (rs.fog_end != rs.fog_start) ? (rs.fog_end - fog_coord) / (rs.fog_end - rs.fog_start) : 1.0f;
+        f = (end != start) ? (end - fog_coord) / (end - start) : 1.0f;
         break;
-    case GL_EXP: f = expf(-rs.fog_density * fog_coord); break;
+    case GL_EXP: f = expf(-density * fog_coord); break;
     case GL_EXP2: {
-        float d = rs.fog_density * fog_coord;
+        float d = density * fog_coord;
         f = expf(-d * d);
         break;
     }
@@ -532,6 +571,11 @@ __device__ __forceinline__ float fog_factor(const mtgl_raster_state &rs, float f
     if (f < 0.0f) f = 0.0f;
     if (f > 1.0f) f = 1.0f;
     return f;
+}
+
+__device__ __forceinline__ float fog_factor(const mtgl_raster_state &rs, float fog_coord)
+{
+    return fog_factor(rs.fog_mode, rs.fog_density, rs.fog_start, rs.fog_end, fog_coord);
 }
 
 // the double-precision depth range map, out of line: inlined, its few FP64 instructions
@@ -550,18 +594,23 @@ __device__ __forceinline__ float map_depth(const DevRaster &R, float z)
     return map_depth_range(t, R.rs.depth_near, R.rs.depth_far);
 }
 
-// write_pixel_masked (raster.c:20-45) on a packed destination pixel
+// write_pixel_masked (raster.c:20-45) on a packed destination pixel; mask bit i: channel i
+__device__ __forceinline__ uint32_t masked_write(uint32_t mask, uint32_t dst, float4 c)
+{
+    if (mask == 15u) return pack_rgba(c.x, c.y, c.z, c.w);
+    if (mask == 0u) return dst;
+    float4 d = unpack_rgba(dst);
+    if (mask & 1u) d.x = c.x;
+    if (mask & 2u) d.y = c.y;
+    if (mask & 4u) d.z = c.z;
+    if (mask & 8u) d.w = c.w;
+    return pack_rgba(d.x, d.y, d.z, d.w);
+}
+
 __device__ __forceinline__ uint32_t masked_write(const mtgl_raster_state &rs, uint32_t dst, float4 c)
 {
     const uint32_t *m = rs.color_mask;
-    if (m[0] && m[1] && m[2] && m[3]) return pack_rgba(c.x, c.y, c.z, c.w);
-    if (!m[0] && !m[1] && !m[2] && !m[3]) return dst;
-    float4 d = unpack_rgba(dst);
-    if (m[0]) d.x = c.x;
-    if (m[1]) d.y = c.y;
-    if (m[2]) d.z = c.z;
-    if (m[3]) d.w = c.w;
-    return pack_rgba(d.x, d.y, d.z, d.w);
+    return masked_write((m[0] ? 1u : 0u) | (m[1] ? 2u : 0u) | (m[2] ? 4u : 0u) | (m[3] ? 8u : 0u), dst, c);
 }
 
 }  // namespace mtgl

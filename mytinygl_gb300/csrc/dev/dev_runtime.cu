@@ -86,6 +86,16 @@ void pack_frag_state(DevRaster &R)
     f.color_mask = mask;
     memcpy(f.fog_color, rs.fog_color, sizeof(f.fog_color));
     memcpy(f.tex_env_color, rs.tex_env_color, sizeof(f.tex_env_color));
+    f.tex = R.tex;
+    f.mip1 = R.mip1;
+    f.tex_w = R.tex_w;
+    f.tex_h = R.tex_h;
+    f.mip_w = R.mip_w;
+    f.mip_h = R.mip_h;
+    f.wrap_s = rs.tex_wrap_s;
+    f.wrap_t = rs.tex_wrap_t;
+    f.min_filter = rs.tex_min_filter;
+    f.mag_filter = rs.tex_mag_filter;
 }
 
 uint32_t push_raster(mtgl_dev *d, const mtgl_raster_state *rs)

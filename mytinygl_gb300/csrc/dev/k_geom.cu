@@ -575,7 +575,7 @@ __device__ __forceinline__ uint32_t vertex_point(const DevRaster &R, uint32_t ra
     const float depth = map_depth(R, nz);
     float4 c = v.col;
     if (R.tex) {
-        const float4 tc = unpack_rgba(sample_lod(R, v.uv.x, v.uv.y, 0.0f));
+        const float4 tc = unpack_rgba(sample_lod(R.fs, v.uv.x, v.uv.y, 0.0f));
         if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) return 0;
         c = make_float4(c.x * tc.x, c.y * tc.y, c.z * tc.z, c.w * tc.w);
     } else if (rs.alpha_test && !cmp_pass(rs.alpha_func, c.w, rs.alpha_ref)) {

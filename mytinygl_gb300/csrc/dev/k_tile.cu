@@ -144,7 +144,7 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, const float *__re
             u = b0 * q8.x + b1 * q8.z + b2 * q9.x;
             v = b0 * q8.y + b1 * q8.w + b2 * q9.y;
         }
-        const float4 tc = unpack_rgba(sample_lod(R, u, v, q4.w));
+        const float4 tc = unpack_rgba(sample_lod(R.fs, u, v, q4.w));
         // the alpha test applies to textured fragments only (raster.c:639-643)
         if ((ctl & FC_ALPHA) && !cmp_pass(__ldg(&S.alpha_func), tc.w, __ldg(&S.alpha_ref))) return false;
         switch (__ldg(&S.tex_env_mode)) {
@@ -251,7 +251,7 @@ __device__ __noinline__ PixelOut shade_prim(const TileArgs &A, const float *r, i
     if (R.tex) {
         const float u = r[R_UV0] + t * (r[R_UV1] - r[R_UV0]);
         const float v = r[R_UV0 + 1] + t * (r[R_UV1 + 1] - r[R_UV0 + 1]);
-        const float4 tc = unpack_rgba(sample_lod(R, u, v, 0.0f));
+        const float4 tc = unpack_rgba(sample_lod(R.fs, u, v, 0.0f));
         // the reference never leaves its loop when this test fails (raster.c:175, 183 skip the
         // Bresenham step); here the pixel is dropped
         if (rs.alpha_test && !cmp_pass(rs.alpha_func, tc.w, rs.alpha_ref)) return none;

@@ -102,7 +102,7 @@ struct DevDraw {
 };
 
 // The fragment stages' part of a raster state, packed for the tile kernel: a word of the
-// stage enables and each stage's operands in 16-byte groups, one 128-byte line in all. The
+// stage enables and each stage's operands in 16-byte groups, 160 bytes in all. The
 // full state spans about a kilobyte (mostly lights and materials) and scatters these fields
 // over several lines; per fragment the kernel now loads the first group, and further groups
 // only for the stages its enables switch on.
@@ -125,13 +125,16 @@ struct __align__(16) FragState {
     uint32_t pad0;
     float fog_color[4];
     float tex_env_color[4];
-    uint32_t pad1[4];
+    const uint32_t *tex, *mip1;            // texture: levels 0 and 1 (see DevRaster)
+    int32_t tex_w, tex_h, mip_w, mip_h;
+    int32_t wrap_s, wrap_t, min_filter, mag_filter;
 };
 
-static_assert(sizeof(FragState) == 128 && offsetof(FragState, stencil_func) == 16 &&
+static_assert(sizeof(FragState) == 160 && offsetof(FragState, stencil_func) == 16 &&
                   offsetof(FragState, stencil_fail) == 32 && offsetof(FragState, blend_src) == 48 &&
                   offsetof(FragState, fog_start) == 64 && offsetof(FragState, fog_color) == 80 &&
-                  offsetof(FragState, tex_env_color) == 96,
+                  offsetof(FragState, tex_env_color) == 96 && offsetof(FragState, tex) == 112 &&
+                  offsetof(FragState, tex_w) == 128 && offsetof(FragState, wrap_s) == 144,
               "FragState groups are read as 16-byte words");
 
 // Raster state with the bound texture resolved to device pointers.
@@ -424,12 +427,20 @@ __device__ __forceinline__ uint32_t sample_level(const TexView &t, int32_t ws, i
     return __ldg(t.px + (size_t)y * t.w + x);
 }
 
-__device__ __forceinline__ uint32_t sample_mip1(const DevRaster &R, float u, float v, int32_t filter)
+// a pointer field through the read-only path
+__device__ __forceinline__ const uint32_t *ldg_ptr(const uint32_t *const *p)
 {
-    if (!R.mip1) return 0xFFFFFFFFu;  // level 1 cannot be built (textures.c:317, 416-419)
-    TexView m{R.mip1, R.mip_w, R.mip_h};
+    return reinterpret_cast<const uint32_t *>(__ldg(reinterpret_cast<const unsigned long long *>(p)));
+}
+
+__device__ __forceinline__ uint32_t sample_mip1(const FragState &S, int32_t ws, int32_t wt, float u, float v,
+                                                int32_t filter)
+{
+    const uint32_t *mip1 = ldg_ptr(&S.mip1);
+    if (!mip1) return 0xFFFFFFFFu;  // level 1 cannot be built (textures.c:317, 416-419)
+    TexView m{mip1, __ldg(&S.mip_w), __ldg(&S.mip_h)};
     bool lin = filter == GL_LINEAR || filter == GL_LINEAR_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_LINEAR;
-    return sample_level(m, R.rs.tex_wrap_s, R.rs.tex_wrap_t, u, v, lin);
+    return sample_level(m, ws, wt, u, v, lin);
 }
 
 // (float)x86_f2i(f): the truncated value as a float (INT32_MIN outside the int range)
@@ -441,9 +452,11 @@ __device__ __forceinline__ float trunc_f2i_f(float f)
     return f < 0.0f ? -t : t;  // a -0 here only meets u - t, where it acts as +0
 }
 
-__device__ inline uint32_t sample_lod(const DevRaster &R, float u, float v, float lod)
+// texture_sample_lod (textures.c:457-557) on the packed texture state
+__device__ inline uint32_t sample_lod(const FragState &S, float u, float v, float lod)
 {
-    const int32_t ws = R.rs.tex_wrap_s, wt = R.rs.tex_wrap_t;
+    const int4 mode = __ldg(reinterpret_cast<const int4 *>(&S.wrap_s));  // wrap s, wrap t, min, mag filter
+    const int32_t ws = mode.x, wt = mode.y;
     if (ws == GL_REPEAT) {
         u = u - trunc_f2i_f(u);
         if (u < 0) u += 1.0f;
@@ -458,25 +471,26 @@ __device__ inline uint32_t sample_lod(const DevRaster &R, float u, float v, floa
         if (v < 0.0f) v = 0.0f;
         if (v > 1.0f) v = 1.0f;
     }
-    int32_t filter = (lod > 0.0f) ? R.rs.tex_min_filter : R.rs.tex_mag_filter;
-    TexView base{R.tex, R.tex_w, R.tex_h};
+    int32_t filter = (lod > 0.0f) ? mode.z : mode.w;
     if (filter == GL_NEAREST_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_NEAREST) {
-        if (lod >= 0.5f) return sample_mip1(R, u, v, filter);
+        if (lod >= 0.5f) return sample_mip1(S, ws, wt, u, v, filter);
         filter = (filter == GL_NEAREST_MIPMAP_NEAREST) ? GL_NEAREST : GL_LINEAR;
     } else if (filter == GL_NEAREST_MIPMAP_LINEAR || filter == GL_LINEAR_MIPMAP_LINEAR) {
         // From lod 1 up the weight of level 1 is 1: lerp_col(c0, c1, 1) gives c1's channels
         // exactly (c0 * 0 + c1 * 1), and packing them gives c1 back (truncating
         // ((float)b / 255) * 255 returns b for every byte), so level 0 is not sampled.
-        if (lod >= 1.0f) return sample_mip1(R, u, v, filter);
+        if (lod >= 1.0f) return sample_mip1(S, ws, wt, u, v, filter);
         if (lod > 0.0f) {
             float cl = (lod > 1.0f) ? 1.0f : lod;
+            const TexView base{ldg_ptr(&S.tex), __ldg(&S.tex_w), __ldg(&S.tex_h)};
             uint32_t c0 = sample_level(base, ws, wt, u, v, filter == GL_LINEAR_MIPMAP_LINEAR);
-            uint32_t c1 = sample_mip1(R, u, v, filter);
+            uint32_t c1 = sample_mip1(S, ws, wt, u, v, filter);
             float4 r = lerp_col(unpack_rgba(c0), unpack_rgba(c1), cl);
             return pack_rgba(r.x, r.y, r.z, r.w);
         }
         filter = (filter == GL_NEAREST_MIPMAP_LINEAR) ? GL_NEAREST : GL_LINEAR;
     }
+    const TexView base{ldg_ptr(&S.tex), __ldg(&S.tex_w), __ldg(&S.tex_h)};
     return sample_level(base, ws, wt, u, v, filter == GL_LINEAR);
 }
 

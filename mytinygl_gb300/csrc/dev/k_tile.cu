@@ -302,8 +302,8 @@ constexpr int tile_min_blocks()
 template <int TS, bool TEX, bool EYE, bool ROUNDS>
 __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(TileArgs A)
 {
-    constexpr int kThreads = TS * TS;
     constexpr int kWarpsX = TS / 8;  // 8x4-pixel warp blocks per tile row band
+    constexpr uint32_t kNoTile = 0xFFFFFFFFu, kSkipTile = 0xFFFFFFFEu;
     __shared__ uint32_t s_tile, s_frame;
 
     if (A.guard && (A.guard[0] > A.records_cap || A.guard[1] > A.pairs_cap)) return;
@@ -313,41 +313,47 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
     const bool have_eye = EYE && A.eye_records != nullptr;
     uint32_t frags = 0;
 
-    for (uint32_t item = blockIdx.x;;) {
-        if (A.ctas) {
-            if (threadIdx.x == 0) {
+    for (bool first = true;; first = false) {
+        if (!A.ctas && !first) break;  // one tile per CTA
+        // Thread 0 takes the next work item and resolves its tile and frame; two barriers per
+        // tile (the previous tile is done; the new one is published).
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t it, hi;
+            if (A.ctas) {
                 // this launch's items: the small-record part of the list, or the rest
                 const uint32_t split = A.split ? min(*A.split, A.ntiles) : (ROUNDS ? A.ntiles : 0u);
-                const uint32_t lo = ROUNDS ? 0u : split, hi = ROUNDS ? split : A.ntiles;
-                const uint32_t it = lo + atomicAdd(A.queue + (ROUNDS ? 0 : 1), 1u);
-                s_tile = it < hi ? it : 0xFFFFFFFFu;
+                hi = ROUNDS ? split : A.ntiles;
+                it = (ROUNDS ? 0u : split) + atomicAdd(A.queue + (ROUNDS ? 0 : 1), 1u);
+            } else {
+                it = blockIdx.x;
+                hi = A.ntiles;
             }
-            __syncthreads();
-            item = s_tile;
-            __syncthreads();
-            if (item == 0xFFFFFFFFu) break;
-        } else if (item >= A.ntiles) {
-            break;
-        }
-        const uint32_t tile = A.order ? A.order[item] : item;
-        if (!A.ctas) item = A.ntiles;  // one tile per CTA
-        // unordered classified launches: each takes the tiles of its own class, in tile order
-        if (A.tile_area && tile_class(A.tile_count, A.tile_area, tile, A.tile_shift) != (ROUNDS ? 0u : 1u)) continue;
-        // the frame owning the tile: last frame whose tile_base <= tile
-        uint32_t f = 0;
-        if (A.nframes > 1) {
-            if (threadIdx.x == 0) {
-                uint32_t lo = 0, hi = A.nframes - 1;
-                while (lo < hi) {
-                    const uint32_t mid = (lo + hi + 1) >> 1;
-                    if (A.frames[mid].tile_base <= tile) lo = mid;
-                    else hi = mid - 1;
+            uint32_t tile = kNoTile, f = 0;
+            if (it < hi) {
+                tile = A.order ? A.order[it] : it;
+                // unordered classified launches take the tiles of their own class, in tile order
+                if (A.tile_area && tile_class(A.tile_count, A.tile_area, tile, A.tile_shift) != (ROUNDS ? 0u : 1u))
+                    tile = kSkipTile;
+                // the frame owning the tile: last frame whose tile_base <= tile
+                if (tile != kSkipTile && A.nframes > 1) {
+                    uint32_t flo = 0, fhi = A.nframes - 1;
+                    while (flo < fhi) {
+                        const uint32_t mid = (flo + fhi + 1) >> 1;
+                        if (A.frames[mid].tile_base <= tile) flo = mid;
+                        else fhi = mid - 1;
+                    }
+                    f = flo;
                 }
-                s_frame = lo;
             }
-            __syncthreads();
-            f = s_frame;
+            s_tile = tile;
+            s_frame = f;
         }
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile == kNoTile) break;
+        if (tile == kSkipTile) continue;
+        const uint32_t f = s_frame;
         const DevFrame &F = A.frames[f];
         const uint32_t count = A.tile_count[tile];
         const ClearOp *clears = A.clears + F.clear_base;

@@ -147,23 +147,30 @@ __global__ void __launch_bounds__(256) k_bin_count(BinArgs A)
     }
 }
 
-// one warp per record: lanes write the record's tiles row-major (pairs stay in submission order)
+// A group of L lanes per record (L = 32 / G, G records per warp from the average tiles per
+// record: 1 for large triangles, up to 8 for small ones, so that a warp has several records'
+// loads in flight): the group writes its record's tiles row-major (pairs stay in submission
+// order).
 __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
 {
     const uint32_t n = records_in(A);
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+    const uint32_t avg = n ? max(1u, *A.total_dev / n) : 1u;
+    const uint32_t G = avg >= 32u ? 1u : (avg >= 16u ? 2u : (avg >= 8u ? 4u : 8u));
+    const uint32_t L = 32u / G;
+    const uint32_t lane = threadIdx.x & 31u, sub = lane / L, sl = lane % L;
+    const uint32_t groups = gridDim.x * (blockDim.x >> 5) * G;
+    for (uint32_t r = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * G + sub; r < n; r += groups) {
         int tx0, ty0, tx1, ty1;
-        const DevFrame &F = rec_tile_box(A.records + (size_t)r * kRecWords, A, tx0, ty0, tx1, ty1);
-        const float4 b1 = __ldg(reinterpret_cast<const float4 *>(A.records + (size_t)r * kRecWords) + 1);
-        const float4 b2 = __ldg(reinterpret_cast<const float4 *>(A.records + (size_t)r * kRecWords) + 2);
+        const float *rec = A.records + (size_t)r * kRecWords;
+        const DevFrame &F = rec_tile_box(rec, A, tx0, ty0, tx1, ty1);
+        const float4 b1 = __ldg(reinterpret_cast<const float4 *>(rec) + 1);
+        const float4 b2 = __ldg(reinterpret_cast<const float4 *>(rec) + 2);
         const int bx0 = __float_as_int(b1.z), by0 = __float_as_int(b1.w);
         const int bx1 = __float_as_int(b2.x), by1 = __float_as_int(b2.y);
         const int w = tx1 - tx0 + 1;
         const int cnt = w * (ty1 - ty0 + 1);
         const uint32_t base = A.rec_tiles[r];
-        for (int i = lane; i < cnt; i += 32) {
+        for (int i = (int)sl; i < cnt; i += (int)L) {
             if (base + (uint32_t)i >= A.npairs) break;
             const int tx = tx0 + i % w, ty = ty0 + i / w;
             const uint32_t tile = F.tile_base + (uint32_t)(ty * F.dims.tiles_x + tx);

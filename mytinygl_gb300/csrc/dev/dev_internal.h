@@ -142,6 +142,7 @@ struct Tables {
     uint32_t slots = 0, tris = 0, ntiles = 0;
     int tile_shift = kTileShiftPlain;
     bool eye = false, any_texture = false;
+    bool defer = false;  // every record a filled triangle whose colour can be deferred (k_tile.cuh)
 };
 
 // Appends the tables of `frames` to `st` and makes the device staging copy large enough.

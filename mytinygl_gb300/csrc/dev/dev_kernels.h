@@ -122,6 +122,7 @@ struct TileArgs {
     const uint32_t *guard;
     uint32_t records_cap, pairs_cap;
     unsigned long long *fragments;
+    int32_t defer;               // every record is a filled triangle with deferrable colour (k_tile.cuh)
 };
 
 // K4: CTAs take tiles from the work queue; for each: clears, then every triangle of the

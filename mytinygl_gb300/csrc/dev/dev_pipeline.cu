@@ -292,12 +292,17 @@ int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframe
     ClearOp *hcl = reinterpret_cast<ClearOp *>(st.p + t.off_clears);
     DevFrame *hfr = reinterpret_cast<DevFrame *>(st.p + t.off_frames);
     uint32_t di = 0, vsb = 0, rsb = 0, clb = 0, slot_base = 0, tri_base = 0, tile_base = 0;
+    bool defer = true;
     for (uint32_t f = 0; f < nframes; f++) {
         const Pass &p = *frames[f].pass;
         const mtgl_dev *d = frames[f].dev;
         uint8_t *data = ds + frames[f].data_off;
         for (const PendingDraw &pd : p.draws) {
             DevDraw dd = pd.d;
+            if (dd.mode < GL_TRIANGLES || dd.mode > GL_POLYGON || dd.raster >= p.rasters.size() ||
+                p.rasters[dd.raster].rs.polygon_mode_front != GL_FILL ||
+                p.rasters[dd.raster].rs.polygon_mode_back != GL_FILL)
+                defer = false;  // points and lines read the stored colour
             if (pd.off_pos >= 0) dd.pos.ptr = data + pd.off_pos;
             if (pd.off_color >= 0) dd.color.ptr = data + pd.off_color;
             if (pd.off_tex >= 0) dd.tex.ptr = data + pd.off_tex;
@@ -318,6 +323,9 @@ int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframe
             DevRaster R = p.rasters[i];
             R.frame = f;
             t.any_texture = t.any_texture || R.tex != nullptr;
+            const uint32_t c = R.fs.ctl;
+            if ((c & FC_BLEND) || ((c & FC_ALPHA) && (c & FC_TEXTURE)) || !(c & (FC_MASK_ALL | FC_MASK_NONE)))
+                defer = false;  // a fragment reads the stored colour, or may be discarded after its depth test
             hrs[rsb + i] = R;
         }
         if (!p.clears.empty()) memcpy(hcl + clb, p.clears.data(), p.clears.size() * sizeof(ClearOp));
@@ -343,6 +351,7 @@ int build_tables(Exec &x, HostStage &st, const FrameSrc *frames, uint32_t nframe
     }
     t.ndraws = (uint32_t)ndraws;
     t.nrasters = (uint32_t)nrs;
+    t.defer = defer && ndraws > 0;
     t.nclears = (uint32_t)ncl;
     t.slots = (uint32_t)slots;
     t.tris = (uint32_t)tris;
@@ -356,6 +365,7 @@ int persistent_ctas(const Exec &x, const Tables &t, int per_sm)
     memset(&probe, 0, sizeof(probe));
     probe.tile_shift = t.tile_shift;
     probe.any_texture = t.any_texture ? 1 : 0;
+    probe.defer = t.defer ? 1 : 0;
     probe.eye_records = t.eye ? reinterpret_cast<const float *>(1) : nullptr;
     const int occ = tile_occupancy(probe);
     const int n = per_sm > 0 ? std::min(per_sm, occ) : occ;
@@ -525,6 +535,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ta.ntiles = ntiles;
     ta.tile_shift = t.tile_shift;
     ta.any_texture = t.any_texture ? 1 : 0;
+    ta.defer = t.defer ? 1 : 0;
     ta.fragments = x.d_frags;
     if (c.ctas) {
         ta.queue = order_aux + kOrderQueues;

@@ -581,6 +581,39 @@ def sc_ragged():
     return s
 
 
+def sc_deferred_colour():
+    """One pass of opaque triangles whose colour the tile kernel defers to the tile's end:
+    heavy overdraw under every depth function, a colour-masked depth pre-pass, depth writes
+    off, stencil updates, and raster states that change between draws (flat / smooth,
+    texture on / off with every env mode and filter, fog, perspective hint)."""
+    s = base("deferred_colour")
+    rng = np.random.default_rng(53)
+    checker_texture(s, 16, seed=21)
+    s.glEnable(G.GL_DEPTH_TEST)
+    s.glEnable(G.GL_STENCIL_TEST)
+    s.glStencilFunc(G.GL_ALWAYS, 3, 0xFF)
+    s.glStencilOp(G.GL_KEEP, G.GL_INCR, G.GL_REPLACE)
+    s.glColorMask(0, 0, 0, 0)  # depth pre-pass: no colour written
+    rand_tris(s, rng, 6, spread=2.0, z=(-5.0, -3.0))
+    s.glColorMask(1, 1, 1, 1)
+    s.glDepthFunc(G.GL_LEQUAL)
+    for k, env in enumerate((G.GL_MODULATE, G.GL_DECAL, G.GL_REPLACE, G.GL_BLEND, G.GL_ADD)):
+        (s.glEnable if k % 2 == 0 else s.glDisable)(G.GL_TEXTURE_2D)
+        s.glTexEnvi(G.GL_TEXTURE_ENV, G.GL_TEXTURE_ENV_MODE, env)
+        s.glTexParameteri(G.GL_TEXTURE_2D, G.GL_TEXTURE_MIN_FILTER,
+                          (G.GL_LINEAR_MIPMAP_LINEAR, G.GL_NEAREST, G.GL_LINEAR_MIPMAP_NEAREST)[k % 3])
+        s.glShadeModel(G.GL_FLAT if k % 3 == 1 else G.GL_SMOOTH)
+        s.glHint(G.GL_PERSPECTIVE_CORRECTION_HINT, G.GL_FASTEST if k == 3 else G.GL_NICEST)
+        (s.glEnable if k >= 2 else s.glDisable)(G.GL_FOG)
+        rand_tris(s, rng, 8, spread=2.2, z=(-6.0, -2.0), uv=True)
+    for func in (G.GL_GREATER, G.GL_ALWAYS, G.GL_NEVER, G.GL_NOTEQUAL, G.GL_LESS):
+        s.glDepthFunc(func)
+        rand_tris(s, rng, 4, spread=2.2, z=(-6.0, -2.0), uv=True)
+    s.glDepthMask(0)
+    rand_tris(s, rng, 4, spread=2.2, z=(-6.0, -2.0), uv=True)
+    return s
+
+
 def sc_vertex_arrays():
     s = base("vertex_arrays")
     rng = np.random.default_rng(30)
@@ -916,6 +949,7 @@ SCENES = {
     "max_width": (sc_max_width, ("lines",)),
     "max_height": (sc_max_height, ("lines",)),
     "ragged": (sc_ragged, ("lines",)),
+    "deferred_colour": (sc_deferred_colour, ()),
     "vertex_arrays": (sc_vertex_arrays, ()),
     "vbo": (sc_vbo, ()),
     "state_in_begin_end": (sc_state_in_begin_end, ()),

@@ -83,20 +83,41 @@ __device__ __forceinline__ float sanitize(float v, bool alpha)
 
 __global__ void __launch_bounds__(128) k_vertex(GeomArgs A)
 {
+    // The vertex state (matrices, lights, materials: about 1.4 KB) is the same for every
+    // slot of a block in the common case; the block then copies it to shared memory once
+    // and reads it from there instead of through L1 per vertex.
+    static_assert(sizeof(mtgl_vertex_state) % 4 == 0 && alignof(mtgl_vertex_state) == 4, "copied as 32-bit words");
+    __shared__ uint32_t s_vs[sizeof(mtgl_vertex_state) / 4];
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= A.total_slots) return;
-    const int d = find_base(A.draw_vslot_base, A.ndraws, g);
-    const DevDraw &D = A.draws[d];
-    const uint32_t k = g - D.vslot_base;
-    int64_t src;
-    uint32_t vsi = D.vs_base;
-    if (D.range_mode) {
-        src = ((int64_t)k < (int64_t)D.range_n) ? D.index_min + (int64_t)k : -1;
-    } else {
-        src = D.index_type ? (int64_t)(int32_t)read_index(D.indices, D.index_type, k) : (int64_t)D.first + k;
-        if (D.vs_ids) vsi += __ldg(D.vs_ids + k);
+    const bool live = g < A.total_slots;
+    int d = 0;
+    uint32_t k = 0, vsi = 0;
+    int64_t src = -1;
+    if (live) {
+        d = find_base(A.draw_vslot_base, A.ndraws, g);
+        const DevDraw &D0 = A.draws[d];
+        k = g - D0.vslot_base;
+        vsi = D0.vs_base;
+        if (D0.range_mode) {
+            src = ((int64_t)k < (int64_t)D0.range_n) ? D0.index_min + (int64_t)k : -1;
+        } else {
+            src = D0.index_type ? (int64_t)(int32_t)read_index(D0.indices, D0.index_type, k) : (int64_t)D0.first + k;
+            if (D0.vs_ids) vsi += __ldg(D0.vs_ids + k);
+        }
     }
-    const mtgl_vertex_state &V = A.vstates[vsi];
+    __shared__ uint32_t s_vsi;
+    if (threadIdx.x == 0) s_vsi = vsi;
+    __syncthreads();
+    const bool shared_vs = __syncthreads_and(!live || vsi == s_vsi) != 0;
+    if (shared_vs) {
+        const uint32_t *src_vs = reinterpret_cast<const uint32_t *>(A.vstates + s_vsi);
+        for (uint32_t i = threadIdx.x; i < sizeof(mtgl_vertex_state) / 4; i += blockDim.x) s_vs[i] = __ldg(src_vs + i);
+        __syncthreads();
+    }
+    if (!live) return;
+    const DevDraw &D = A.draws[d];
+    const mtgl_vertex_state &V =
+        shared_vs ? *reinterpret_cast<const mtgl_vertex_state *>(s_vs) : A.vstates[vsi];
 
     float p[4], c[4], t[2], n[3];
     fetch_attr<4>(D.pos, src, p);

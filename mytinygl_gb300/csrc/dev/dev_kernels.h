@@ -8,6 +8,8 @@
 
 namespace mtgl {
 
+constexpr uint32_t kClipClasses = 96;  // one-plane candidates: first plane x in/out pattern; the rest
+
 struct GeomArgs {
     const DevDraw *draws;
     const uint32_t *draw_vslot_base;  // per draw, ascending
@@ -27,6 +29,9 @@ struct GeomArgs {
     float *eye_records;               // emit pass output, kEyeWords per record (may be null)
     uint32_t records_cap;             // records the output buffers hold (writes beyond are dropped)
     uint32_t *clip_list;              // triangles that straddle a clip plane (total_tris entries)
+    uint32_t *clip_class;             // per entry: clip class << 24 | rank within the class
+    uint32_t *clip_sorted;            // the entries grouped by class (null: process clip_list as is)
+    uint32_t *class_count;            // kClipClasses counters (zeroed by the count launch)
     uint32_t *clip_count;             // their number (device; zeroed by the count launch)
     int32_t sms;
 };

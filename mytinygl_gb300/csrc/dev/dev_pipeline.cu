@@ -396,8 +396,9 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if (eye && (rc = sc.take(S_EYES, slots, &eyes))) return rc;
     if ((rc = sc.take(S_TRI_COUNTS, tris, &tri_counts))) return rc;
     if ((rc = sc.take(S_TRI_OFFSETS, tris, &tri_offsets))) return rc;
+    // clip list, its class words, the class-sorted list and the class counters
     uint32_t *clip_list = nullptr;
-    if ((rc = sc.take(S_CLIP_LIST, tris, &clip_list))) return rc;
+    if ((rc = sc.take(S_CLIP_LIST, 3 * (size_t)tris + kClipClasses, &clip_list))) return rc;
     // tile counts, then (persistent ordered launches) the per-tile record-box coverage
     if ((rc = sc.take(S_TILE_COUNT, 2 * ((size_t)ntiles + 1), &tile_count))) return rc;
     uint32_t *tile_area = (c.ctas && (c.order || c.classify)) ? tile_count + ntiles + 1 : nullptr;
@@ -441,6 +442,10 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ga.tri_counts = tri_counts;
     ga.tri_offsets = tri_offsets;
     ga.clip_list = clip_list;
+    ga.clip_class = clip_list + tris;
+    // sort by class while a class rank fits the class word's 24 bits
+    ga.clip_sorted = tris < (1u << 24) ? clip_list + 2 * (size_t)tris : nullptr;
+    ga.class_count = clip_list + 3 * (size_t)tris;
     ga.clip_count = x.d_totals + 4;
     ga.sms = x.sms;
     int launches = 0;

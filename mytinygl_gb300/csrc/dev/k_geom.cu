@@ -331,6 +331,20 @@ __device__ __forceinline__ int clip_one_plane(const V &v0, const V &v1, const V 
     return n;
 }
 
+// The clip list is processed grouped by these classes, so that a warp's lanes take the same
+// path: for a triangle whose vertices are all inside every plane after its first crossed
+// plane p (nearly always clipped in registers), 8 * p + its in/out pattern at p; 48 + the
+// same for the others.
+__device__ __forceinline__ uint32_t clip_class(const float4 &a, const float4 &b, const float4 &c, int p)
+{
+    uint32_t later = 0;
+    for (int q = p + 1; q < 6; q++)
+        if (!(plane_dist(a, q) >= 0.0f && plane_dist(b, q) >= 0.0f && plane_dist(c, q) >= 0.0f)) later = 48;
+    const uint32_t m = (plane_dist(a, p) >= 0.0f ? 1u : 0u) | (plane_dist(b, p) >= 0.0f ? 2u : 0u) |
+                       (plane_dist(c, p) >= 0.0f ? 4u : 0u);
+    return later + 8u * (uint32_t)p + m;
+}
+
 // clip_triangle (clipping.h:106-126): Sutherland-Hodgman passes from plane `first` on (the
 // earlier ones copy the triangle unchanged, see clip_start); result in bufA[0..n)
 template <class V>
@@ -924,6 +938,8 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
     const DevRaster &R = *P.R;
     const RecOut o = rec_out(A, t, EMIT, EYE);
     uint32_t produced = 0;
+    bool straddles = false;  // count pass: goes to the clip list, with its clip class
+    uint32_t cls = 0;
 
     if (D.mode == GL_POINTS) {
         V v;
@@ -951,12 +967,41 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
             produced = setup_fan_tri(R, D.raster, P.frame, P.dims, v0, v1, v2, o, 0);
         } else if (start != kClipEmpty) {
             if (EMIT) return;  // k_clip emits it
-            const uint32_t slot = atomicAdd(A.clip_count, 1u);
-            if (slot < A.total_tris) A.clip_list[slot] = t;
-            return;  // k_clip stores its count
+            cls = A.clip_sorted ? clip_class(v0.clip, v1.clip, v2.clip, start) : 0u;
+            straddles = true;
         }
     }
-    if (!EMIT) A.tri_counts[t] = produced;
+    if (EMIT) return;
+    // Straddling triangles go to the clip list (k_clip stores their counts). The appends are
+    // combined per warp: one atomic for the list, one per class present in the warp.
+    const uint32_t active = __activemask();
+    const uint32_t want = __ballot_sync(active, straddles);
+    if (want) {
+        const int lane = (int)(threadIdx.x & 31u);
+        const uint32_t below = (1u << lane) - 1u;
+        const int first = __ffs(want) - 1;
+        uint32_t base = 0;
+        if (lane == first) base = atomicAdd(A.clip_count, (uint32_t)__popc(want));
+        base = __shfl_sync(active, base, first);
+        uint32_t rank = 0;
+        if (A.clip_sorted) {
+            const uint32_t peers = __match_any_sync(active, straddles ? cls : 0xFFFFFFFFu);
+            const int leader = __ffs(peers) - 1;
+            uint32_t rb = 0;
+            if (straddles && lane == leader) rb = atomicAdd(A.class_count + cls, (uint32_t)__popc(peers));
+            rb = __shfl_sync(active, rb, leader);
+            rank = rb + (uint32_t)__popc(peers & below);
+        }
+        if (straddles) {
+            const uint32_t slot = base + (uint32_t)__popc(want & below);
+            if (slot < A.total_tris) {
+                A.clip_list[slot] = t;
+                if (A.clip_sorted) A.clip_class[slot] = (cls << 24) | rank;
+            }
+            return;
+        }
+    }
+    A.tri_counts[t] = produced;
 }
 
 // The listed triangles: Sutherland-Hodgman from the first plane that is not all-inside, then
@@ -967,8 +1012,9 @@ __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
 {
     using V = CVx<EYE>;
     const uint32_t n = min(*A.clip_count, A.total_tris);
+    const uint32_t *list = A.clip_sorted ? A.clip_sorted : A.clip_list;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t t = A.clip_list[i];
+        const uint32_t t = list[i];
         if (EMIT && A.tri_counts[t] == 0) continue;
         const Prim<EYE> P = prim_of<EYE>(A, t);
         const DevDraw &D = *P.D;
@@ -1004,6 +1050,26 @@ __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
     }
 }
 
+// groups the clip list by class (clip_class): entry i goes to its class's start + its rank
+__global__ void __launch_bounds__(256) k_clip_sort(GeomArgs A)
+{
+    const uint32_t n = min(*A.clip_count, A.total_tris);
+    if (blockIdx.x * blockDim.x >= n) return;  // no entries for this block (uniform)
+    __shared__ uint32_t count[kClipClasses], start[kClipClasses];
+    if (threadIdx.x < kClipClasses) count[threadIdx.x] = A.class_count[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < kClipClasses) {  // exclusive prefix of the class counts, from shared memory
+        uint32_t run = 0;
+        for (uint32_t c = 0; c < threadIdx.x; c++) run += count[c];
+        start[threadIdx.x] = run;
+    }
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t w = A.clip_class[i];
+        A.clip_sorted[start[w >> 24] + (w & 0xFFFFFFu)] = A.clip_list[i];
+    }
+}
+
 int launch_vertex(const GeomArgs &a, cudaStream_t s)
 {
     if (!a.total_slots) return 0;
@@ -1024,14 +1090,16 @@ template <bool EMIT>
 int launch_setup(const GeomArgs &a, cudaStream_t s)
 {
     const unsigned g = (a.total_tris + 127) / 128;
-    if (a.eyes) {
-        k_setup<EMIT, true><<<g, 128, 0, s>>>(a);
-        k_clip<EMIT, true><<<clip_grid(a), 64, 0, s>>>(a);
-    } else {
-        k_setup<EMIT, false><<<g, 128, 0, s>>>(a);
-        k_clip<EMIT, false><<<clip_grid(a), 64, 0, s>>>(a);
+    int launches = 2;
+    if (a.eyes) k_setup<EMIT, true><<<g, 128, 0, s>>>(a);
+    else k_setup<EMIT, false><<<g, 128, 0, s>>>(a);
+    if (!EMIT && a.clip_sorted) {  // the count pass groups the list once; the emit pass reuses it
+        k_clip_sort<<<clip_grid(a), 256, 0, s>>>(a);
+        launches++;
     }
-    return 2;
+    if (a.eyes) k_clip<EMIT, true><<<clip_grid(a), 64, 0, s>>>(a);
+    else k_clip<EMIT, false><<<clip_grid(a), 64, 0, s>>>(a);
+    return launches;
 }
 
 }  // namespace
@@ -1040,6 +1108,7 @@ int launch_setup_count(const GeomArgs &a, cudaStream_t s)
 {
     if (!a.total_tris) return 0;
     cudaMemsetAsync(a.clip_count, 0, sizeof(uint32_t), s);
+    if (a.clip_sorted) cudaMemsetAsync(a.class_count, 0, kClipClasses * sizeof(uint32_t), s);
     return launch_setup<false>(a, s);
 }
 

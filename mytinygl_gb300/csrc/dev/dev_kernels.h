@@ -81,6 +81,10 @@ int launch_bin_expand(const BinArgs &a, cudaStream_t s);
 // as ping-pong storage.
 int launch_bin_sort(BinArgs &a, cudaStream_t s);
 size_t radix_hist_words(uint32_t npairs);
+// Each tile's range of the sorted pairs: tile_start and tile_count (zero for a tile with no
+// pairs), read off the sorted keys where the tile id changes. tile_start and tile_count must
+// be zero for every tile on entry.
+int launch_tile_ranges(const BinArgs &a, cudaStream_t s);
 
 // Work order of the persistent tile launches. Tiles whose records are small (their boxes
 // cover on average less than a quarter of the tile) come first, then the others; each group

@@ -476,6 +476,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
 
     // ---- binning
     CK(cudaMemsetAsync(tile_count, 0, (tile_area ? 2 : 1) * ((size_t)ntiles + 1) * sizeof(uint32_t), s));
+    CK(cudaMemsetAsync(tile_start, 0, ((size_t)ntiles + 1) * sizeof(uint32_t), s));
     BinArgs ba;
     memset(&ba, 0, sizeof(ba));
     ba.records = records;
@@ -519,10 +520,10 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
         ba.npairs = pair_cap;
         launches += launch_bin_expand(ba, s);
         launches += launch_bin_sort(ba, s);
+        launches += launch_tile_ranges(ba, s);
     } else {
         CK(cudaMemsetAsync(x.d_totals + 1, 0, sizeof(uint32_t), s));
     }
-    launches += launch_scan(tile_count, tile_start, ntiles, scan_temp, x.d_totals + 2, s);
     x.prof_mark();
 
     TileArgs ta;

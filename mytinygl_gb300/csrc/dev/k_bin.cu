@@ -176,7 +176,6 @@ __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
             const uint32_t tile = F.tile_base + (uint32_t)(ty * F.dims.tiles_x + tx);
             A.keys[base + i] = tile;
             A.vals[base + i] = r;
-            atomicAdd(A.tile_count + tile, 1u);
             if (A.tile_area) {  // pixels of the record's box inside this tile
                 const int sh = A.tile_shift;
                 const int ox = min(bx1, ((tx + 1) << sh) - 1) - max(bx0, tx << sh) + 1;
@@ -193,6 +192,32 @@ unsigned stride_grid(uint64_t threads, unsigned block, int sms)
     const uint64_t want = (threads + block - 1) / block;
     const uint64_t cap = (uint64_t)(sms > 0 ? sms : 1) * 16;
     return (unsigned)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+// Where the sorted tile id changes, the earlier tile's range ends and the later one's
+// starts: the first writes the end position into tile_count, the second its start.
+__global__ void __launch_bounds__(256) k_tile_bounds(BinArgs A)
+{
+    const uint32_t n = min(*A.total_dev, A.npairs);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = A.keys[i];
+        if (i == 0 || A.keys[i - 1] != k) A.tile_start[k] = i;
+        if (i + 1 == n || A.keys[i + 1] != k) A.tile_count[k] = i + 1;
+    }
+}
+
+// end position - start = count; a tile without pairs has both still zero
+__global__ void __launch_bounds__(256) k_tile_counts(BinArgs A)
+{
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < A.ntiles; t += gridDim.x * blockDim.x)
+        A.tile_count[t] -= A.tile_start[t];
+}
+
+int launch_tile_ranges(const BinArgs &a, cudaStream_t s)
+{
+    if (a.npairs) k_tile_bounds<<<stride_grid(a.npairs, 256, a.sms), 256, 0, s>>>(a);
+    k_tile_counts<<<stride_grid(a.ntiles, 256, a.sms), 256, 0, s>>>(a);
+    return a.npairs ? 2 : 1;
 }
 
 int launch_bin_count(const BinArgs &a, cudaStream_t s)

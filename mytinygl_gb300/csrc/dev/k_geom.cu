@@ -862,7 +862,9 @@ __device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t r
     r4[11] = make_float4(a.ez, b.ez, c.ez, __uint_as_float(raster_id));
     // edge_function(a, b, p) = (px - ax) * (by - ay) - (py - ay) * (bx - ax): the per-edge
     // differences are the same floats whether formed per pixel or once here
-    const uint32_t flags = (back ? 1u : 0u) | (zc << 1) | (raises_depth(rs) ? kFlagRaisesDepth : 0u);
+    const uint32_t flags = (back ? 1u : 0u) | (zc << 1) | (raises_depth(rs) ? kFlagRaisesDepth : 0u) |
+                           ((R.fs.ctl & 0xFFFu) << kRecCtlShift) |
+                           (((rs.depth_func - GL_NEVER) & 7u) << kRecDepthFuncShift);
     r4[12] = make_float4(__uint_as_float(flags), fy2 - fy1, fx2 - fx1, fy0 - fy2);
     r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, __uint_as_float(frame));
     if (eyerec) {

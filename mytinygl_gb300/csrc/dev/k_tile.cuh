@@ -194,10 +194,12 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, uint32_t ridx, co
     const float4 q3 = __ldg(r4 + 3);    // Z0 Z1 Z2 DMIN
     const uint32_t ri = __float_as_uint(__ldg(r + R_RASTER));
     const DevRaster &R = A.rasters[min(ri, A.nrasters - 1)];
-    // the fragment stages' packed state: the enables word, then each stage's operands as the
-    // stage needs them (loaded where used, from one cached line, to keep few registers live)
+    // the fragment stages' packed state: the enables and the depth function come with the
+    // record's flags; the other operands are loaded as the stages need them (from one cached
+    // line, to keep few registers live)
     const FragState &S = R.fs;
-    const uint32_t ctl = __ldg(&S.ctl);
+    const uint32_t rflags = __float_as_uint(q12.x);
+    const uint32_t ctl = (rflags >> kRecCtlShift) & 0xFFFu;
     const float z = b0 * q3.x + b1 * q3.y + b2 * q3.z;
     const float t = (z + 1.0f) * 0.5f;
     const float depth = (ctl & FC_DEFAULT_RANGE) ? t : map_depth_range(t, R.rs.depth_near, R.rs.depth_far);
@@ -211,7 +213,7 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, uint32_t ridx, co
             return false;
         }
     }
-    if ((ctl & FC_DEPTH) && !cmp_pass(__ldg(&S.depth_func), depth, dep)) {
+    if ((ctl & FC_DEPTH) && !cmp_pass(GL_NEVER + ((rflags >> kRecDepthFuncShift) & 7u), depth, dep)) {
         if (ctl & FC_STENCIL)
             st = stencil_write(st, stencil_apply(__ldg(&S.stencil_zfail), sv, __ldg(&S.stencil_ref)),
                                __ldg(&S.stencil_writemask));

@@ -60,6 +60,10 @@ constexpr uint32_t kFlagRaisesDepth = 8u;
 //     bbox R_MINX..R_MAXY over the widened line clamped to framebuffer and scissor.
 enum RecType { REC_TRI = 0, REC_POINT = 1, REC_LINE = 2 };
 constexpr int kRecTypeShift = 4;
+// R_FLAGS of a triangle record, bits 8-19: its raster state's FragCtl enables; bits 20-22:
+// its depth function - GL_NEVER. The tile kernel's tests read them with the edge
+// coefficients (same 16-byte word) instead of through the raster state.
+constexpr int kRecCtlShift = 8, kRecDepthFuncShift = 20;
 __device__ __forceinline__ uint32_t rec_type(const float *r) { return (__float_as_uint(r[R_FLAGS]) >> kRecTypeShift) & 3u; }
 
 // Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).

@@ -192,20 +192,23 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, uint32_t ridx, co
     const float inv_area = q2.w;
     const float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
     const float4 q3 = __ldg(r4 + 3);    // Z0 Z1 Z2 DMIN
-    const uint32_t ri = __float_as_uint(__ldg(r + R_RASTER));
-    const DevRaster &R = A.rasters[min(ri, A.nrasters - 1)];
+    // the raster state, only where a stage reads more than the record carries
+    auto raster = [&]() -> const DevRaster & {
+        return A.rasters[min(__float_as_uint(__ldg(r + R_RASTER)), A.nrasters - 1)];
+    };
     // the fragment stages' packed state: the enables and the depth function come with the
     // record's flags; the other operands are loaded as the stages need them (from one cached
     // line, to keep few registers live)
-    const FragState &S = R.fs;
     const uint32_t rflags = __float_as_uint(q12.x);
     const uint32_t ctl = (rflags >> kRecCtlShift) & 0xFFFu;
     const float z = b0 * q3.x + b1 * q3.y + b2 * q3.z;
     const float t = (z + 1.0f) * 0.5f;
-    const float depth = (ctl & FC_DEFAULT_RANGE) ? t : map_depth_range(t, R.rs.depth_near, R.rs.depth_far);
+    const float depth =
+        (ctl & FC_DEFAULT_RANGE) ? t : map_depth_range(t, raster().rs.depth_near, raster().rs.depth_far);
 
     uint32_t sv = 0;
     if (ctl & FC_STENCIL) {
+        const FragState &S = raster().fs;
         const uint4 g = __ldg(reinterpret_cast<const uint4 *>(&S) + 1);  // func, ref, mask, writemask
         sv = st;
         if (!stencil_pass(g.x, (int32_t)g.y, g.z, sv)) {
@@ -214,14 +217,18 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, uint32_t ridx, co
         }
     }
     if ((ctl & FC_DEPTH) && !cmp_pass(GL_NEVER + ((rflags >> kRecDepthFuncShift) & 7u), depth, dep)) {
-        if (ctl & FC_STENCIL)
+        if (ctl & FC_STENCIL) {
+            const FragState &S = raster().fs;
             st = stencil_write(st, stencil_apply(__ldg(&S.stencil_zfail), sv, __ldg(&S.stencil_ref)),
                                __ldg(&S.stencil_writemask));
+        }
         return false;
     }
-    if (ctl & FC_STENCIL)
+    if (ctl & FC_STENCIL) {
+        const FragState &S = raster().fs;
         st = stencil_write(st, stencil_apply(__ldg(&S.stencil_zpass), sv, __ldg(&S.stencil_ref)),
                            __ldg(&S.stencil_writemask));
+    }
 
     if (DEFER) {
         if (ctl & FC_MASK_ALL) pend = ridx;  // this fragment's colour replaces the pixel's
@@ -231,6 +238,8 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, uint32_t ridx, co
         }
         return false;
     }
+    const DevRaster &R = raster();
+    const FragState &S = R.fs;
     float4 c;
     if (!frag_color<TEX, EYE>(R, ctl, r4, e, have_eye, b0, b1, b2, c)) return false;
     bool wrote = false;

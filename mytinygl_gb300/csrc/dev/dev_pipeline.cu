@@ -401,7 +401,9 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if ((rc = sc.take(S_CLIP_LIST, 3 * (size_t)tris + kClipClasses, &clip_list))) return rc;
     // tile counts, then (persistent ordered launches) the per-tile record-box coverage
     if ((rc = sc.take(S_TILE_COUNT, 2 * ((size_t)ntiles + 1), &tile_count))) return rc;
-    uint32_t *tile_area = (c.ctas && (c.order || c.classify)) ? tile_count + ntiles + 1 : nullptr;
+    // record-box coverage per tile, for the split between tiles run by rounds and per record;
+    // deferred-colour passes run every tile per record (their fragments are cheap: tests only)
+    uint32_t *tile_area = (c.ctas && (c.order || c.classify) && !t.defer) ? tile_count + ntiles + 1 : nullptr;
     if ((rc = sc.take(S_TILE_START, (size_t)ntiles + 1, &tile_start))) return rc;
     if (c.ctas && c.order && (rc = sc.take(S_ORDER, ntiles, &order))) return rc;
     if (c.ctas && (rc = sc.take(S_ORDER_AUX, kOrderAuxWords, &order_aux))) return rc;

@@ -588,7 +588,7 @@ struct TileVariant {
     static int launch(const TileArgs &a, cudaStream_t s)
     {
         const unsigned grid = a.ctas ? (unsigned)std::min<uint32_t>((uint32_t)a.ctas, a.ntiles) : a.ntiles;
-        if ((a.split || a.tile_area) && a.ctas) {  // small-record tiles by rounds, then the rest per record
+        if ((a.split || a.tile_area) && a.ctas && !DEFER) {  // small-record tiles by rounds, then the rest
             k_tile<TS, TEX, EYE, true, DEFER><<<grid, TS * TS, 0, s>>>(a);
             k_tile<TS, TEX, EYE, false, DEFER><<<grid, TS * TS, 0, s>>>(a);
             return 2;

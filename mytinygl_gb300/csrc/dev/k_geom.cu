@@ -254,20 +254,29 @@ __device__ __forceinline__ void snap_plane(V &v, int p)
 // those extra vertices are dropped instead of written out of bounds.
 constexpr int kClipMax = 12;
 
+// A vertex's inside mask: bit p set when it is inside plane p (plane_dist >= 0; a NaN
+// distance is outside). The planes are constants here, so the six tests are plain adds.
+__device__ __forceinline__ uint32_t inside_mask(const float4 &v)
+{
+    uint32_t m = 0;
+#pragma unroll
+    for (int p = 0; p < 6; p++) m |= (plane_dist(v, p) >= 0.0f ? 1u : 0u) << p;
+    return m;
+}
+constexpr uint32_t kAllInside = 63u;
+
 // Where clip_triangle's six passes can start. A pass over a triangle whose three vertices
 // are all inside its plane copies them unchanged, in order, so passes are skipped while that
 // holds; at the first plane with all three outside the pass returns an empty polygon, so the
-// triangle produces nothing. Returns 0..5 (the first pass that must run), kClipNone (all
-// inside: no clipping) or kClipEmpty.
+// triangle produces nothing. Takes the vertices' inside masks; returns 0..5 (the first pass
+// that must run), kClipNone (all inside: no clipping) or kClipEmpty.
 constexpr int kClipNone = 6, kClipEmpty = 7;
-__device__ __forceinline__ int clip_start(const float4 &a, const float4 &b, const float4 &c)
+__device__ __forceinline__ int clip_start(uint32_t ma, uint32_t mb, uint32_t mc)
 {
-#pragma unroll
-    for (int p = 0; p < 6; p++) {
-        const bool ia = plane_dist(a, p) >= 0.0f, ib = plane_dist(b, p) >= 0.0f, ic = plane_dist(c, p) >= 0.0f;
-        if (!(ia && ib && ic)) return (ia || ib || ic) ? p : kClipEmpty;
-    }
-    return kClipNone;
+    const uint32_t all = ma & mb & mc;
+    if (all == kAllInside) return kClipNone;
+    const int p = __ffs(~all) - 1;  // the first plane not all-inside
+    return ((ma | mb | mc) >> p) & 1u ? p : kClipEmpty;
 }
 
 // The Sutherland-Hodgman pass of plane p over a triangle, in registers, for the common case
@@ -323,25 +332,20 @@ __device__ __forceinline__ int clip_one_plane(const V &v0, const V &v1, const V 
         return 0;
     }
     if (!ok) return 0;
-    for (int q = p + 1; q < 6; q++) {
-        if (!(plane_dist(o0.clip, q) >= 0.0f) || !(plane_dist(o1.clip, q) >= 0.0f) ||
-            !(plane_dist(o2.clip, q) >= 0.0f) || (n == 4 && !(plane_dist(o3.clip, q) >= 0.0f)))
-            return 0;
-    }
-    return n;
+    uint32_t in = inside_mask(o0.clip) & inside_mask(o1.clip) & inside_mask(o2.clip);
+    if (n == 4) in &= inside_mask(o3.clip);
+    const uint32_t later = kAllInside & ~((2u << p) - 1u);  // the planes after p
+    return (in & later) == later ? n : 0;
 }
 
 // The clip list is processed grouped by these classes, so that a warp's lanes take the same
 // path: for a triangle whose vertices are all inside every plane after its first crossed
 // plane p (nearly always clipped in registers), 8 * p + its in/out pattern at p; 48 + the
-// same for the others.
-__device__ __forceinline__ uint32_t clip_class(const float4 &a, const float4 &b, const float4 &c, int p)
+// same for the others. Takes the vertices' inside masks and p = clip_start(...).
+__device__ __forceinline__ uint32_t clip_class(uint32_t ma, uint32_t mb, uint32_t mc, int p)
 {
-    uint32_t later = 0;
-    for (int q = p + 1; q < 6; q++)
-        if (!(plane_dist(a, q) >= 0.0f && plane_dist(b, q) >= 0.0f && plane_dist(c, q) >= 0.0f)) later = 48;
-    const uint32_t m = (plane_dist(a, p) >= 0.0f ? 1u : 0u) | (plane_dist(b, p) >= 0.0f ? 2u : 0u) |
-                       (plane_dist(c, p) >= 0.0f ? 4u : 0u);
+    const uint32_t later = ((~(ma & mb & mc) & kAllInside) >> (p + 1)) ? 48u : 0u;
+    const uint32_t m = ((ma >> p) & 1u) | (((mb >> p) & 1u) << 1) | (((mc >> p) & 1u) << 2);
     return later + 8u * (uint32_t)p + m;
 }
 
@@ -961,7 +965,8 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
         load_cv(A, element_slot(D, e0), v0);
         load_cv(A, element_slot(D, e1), v1);
         load_cv(A, element_slot(D, e2), v2);
-        const int start = clip_start(v0.clip, v1.clip, v2.clip);
+        const uint32_t m0 = inside_mask(v0.clip), m1 = inside_mask(v1.clip), m2 = inside_mask(v2.clip);
+        const int start = clip_start(m0, m1, m2);
         if (start == kClipNone) {  // the clipper would return the triangle unchanged
             persp_divide(v0);
             persp_divide(v1);
@@ -969,7 +974,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
             produced = setup_fan_tri(R, D.raster, P.frame, P.dims, v0, v1, v2, o, 0);
         } else if (start != kClipEmpty) {
             if (EMIT) return;  // k_clip emits it
-            cls = A.clip_sorted ? clip_class(v0.clip, v1.clip, v2.clip, start) : 0u;
+            cls = A.clip_sorted ? clip_class(m0, m1, m2, start) : 0u;
             straddles = true;
         }
     }
@@ -1028,7 +1033,7 @@ __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
         load_cv(A, element_slot(D, e0), v0);
         load_cv(A, element_slot(D, e1), v1);
         load_cv(A, element_slot(D, e2), v2);
-        const int start = clip_start(v0.clip, v1.clip, v2.clip);
+        const int start = clip_start(inside_mask(v0.clip), inside_mask(v1.clip), inside_mask(v2.clip));
         uint32_t produced = 0;
         V bufA[kClipMax];
         int nv = 0;

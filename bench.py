@@ -68,6 +68,7 @@ WORKLOADS["serve"] = dict(builder=None, full_tris=None, name="serve_32_scenes_po
                                 "seed, 40 GiB framebuffer + pipeline-scratch budget"))
 REC_BYTES = 224  # triangle record written by the setup kernel, read by the tile kernel
 BATCH_FRAMES = 256  # frames per step of the batch workload (--frames changes it for profiling)
+E2E_SETS = 3  # context sets the end-to-end batch measurement keeps in flight
 
 
 class Timings(ctypes.Structure):
@@ -490,11 +491,12 @@ def run_batch(args, spec):
 
     # e2e: each step replays every frame's GL calls with client vertex arrays (staged and
     # sent host->device that step) and copies every colour buffer back into page-locked host
-    # memory (mtgl_batch_render_read). Sequential: one step at a time. Two in flight: two
-    # sets of contexts and executors alternate, so one step's host work overlaps the other's
-    # device work, as a renderer feeding frames continuously would run.
+    # memory (mtgl_batch_render_read). Sequential: one step at a time. In flight: E2E_SETS
+    # sets of contexts and executors take turns (triple buffering), so one step's host work
+    # (playing the GL calls, submitting) overlaps the others' copies and device work, as a
+    # renderer feeding frames continuously would run.
     escenes = W.uneven_batch(BATCH_FRAMES, use_vbo=False)
-    e_steps = max(2, min(args.steps, 10))
+    e_steps = max(E2E_SETS, min(args.steps, 20))
 
     def e2e_set():
         c, st = setup_batch_frames(lib, escenes)
@@ -502,7 +504,7 @@ def run_batch(args, spec):
               for sc in escenes]
         return c, st, lib.batch(), hs
 
-    sets = [e2e_set(), e2e_set()]
+    sets = [e2e_set() for _ in range(E2E_SETS)]
     for ectxs, estreams, ebatch, hosts in sets:
         for _ in range(args.warmup):
             estreams.play()
@@ -523,7 +525,7 @@ def run_batch(args, spec):
     e2e_seq_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     for k in range(e_steps):
-        ectxs, estreams, ebatch, hosts = sets[k % 2]
+        ectxs, estreams, ebatch, hosts = sets[k % E2E_SETS]
         ebatch.wait()  # this set's previous step has landed
         estreams.play()
         ebatch.render(ectxs, colors=hosts)
@@ -578,7 +580,7 @@ def run_batch(args, spec):
                      "frac": round(achieved / peak, 5) if achieved else None,
                      "algorithmic_bytes_per_launch": int(k4_bytes), "traffic": ncu_traffic(spec["name"])},
         "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s",
-                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(npix * 4), "steps_in_flight": 2,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(npix * 4), "steps_in_flight": E2E_SETS,
                 "sequential_value": round(e2e_seq_fps, 2),
                 "note": "host clock; GL calls replayed with client arrays every step (their staged bytes are "
                         "h2d), every colour buffer copied to page-locked host memory"},

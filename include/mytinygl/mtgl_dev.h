@@ -230,6 +230,9 @@ typedef struct {
     float pair_factor;       /* initial tile-pair capacity per record; 0: default           */
     int32_t use_graph;       /* 1: capture the run in a CUDA graph and replay it; 0: launch */
     int32_t order_by_cost;   /* 1: hand out the costliest tiles first; 0: in frame order    */
+    int32_t readback_kernel; /* 1: colour read-backs into mapped page-locked host memory are
+                                written by a kernel (one launch per 128 frames); 0: one copy
+                                call per frame. Other destinations are always copied.       */
 } mtgl_batch_config;
 
 typedef struct {

@@ -60,6 +60,8 @@ struct mtgl_batch {
     std::vector<Pass> passes;
     std::vector<FrameSrc> frames;     // frame f renders passes[f] into frames[f].dev
     std::vector<std::pair<mtgl_dev *, uint32_t *>> readbacks;
+    std::vector<ReadbackItem> readback_items;  // scratch of record_after
+    std::vector<mtgl_dev *> uploaded;  // contexts whose staging areas this run's copies read
     // client bytes of the first passes go to the device copy at add time, straight from
     // their context's pinned staging area; the rest are copied into this batch's area
     size_t direct_end = 0;
@@ -79,17 +81,74 @@ struct mtgl_batch {
 
 namespace {
 
+// The device address of [p, p + bytes) when both ends lie in page-locked host memory mapped
+// into the device's address space, else null.
+uint32_t *mapped_host(uint32_t *p, size_t bytes)
+{
+    cudaPointerAttributes a, z;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer ||
+        cudaPointerGetAttributes(&z, reinterpret_cast<char *>(p) + bytes - 1) != cudaSuccess ||
+        z.type != cudaMemoryTypeHost ||
+        z.devicePointer != static_cast<void *>(static_cast<char *>(a.devicePointer) + bytes - 1)) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return static_cast<uint32_t *>(a.devicePointer);
+}
+
+// Colour read-backs, then the run's completion events. Destinations in mapped page-locked
+// memory are written by read-back kernels (one launch per group of frames instead of a copy
+// call per frame); the others are copied.
 int record_after(mtgl_batch *b)
 {
+    std::vector<ReadbackItem> &items = b->readback_items;
+    items.clear();
     for (const auto &rb : b->readbacks) {
         const size_t n = (size_t)rb.first->width * (size_t)rb.first->height;
-        CK(cudaMemcpyAsync(rb.second, rb.first->color, n * 4, cudaMemcpyDeviceToHost, b->x.stream));
+        uint32_t *dst = (b->cfg.readback_kernel && n > 0 && n <= UINT32_MAX) ? mapped_host(rb.second, n * 4) : nullptr;
+        if (dst) items.push_back(ReadbackItem{rb.first->color, dst, (uint32_t)n, 0u});
+        else CK(cudaMemcpyAsync(rb.second, rb.first->color, n * 4, cudaMemcpyDeviceToHost, b->x.stream));
     }
-    for (mtgl_dev *d : b->devs) {
-        CK(cudaEventRecord(d->after_batch, b->x.stream));
-        d->wait_batch = true;
+    if (!items.empty()) {
+        const int k = launch_readback(items.data(), (int)items.size(), b->x.sms, b->x.stream);
+        CK(cudaGetLastError());
+        b->stats.kernel_launches += (uint64_t)k;
+    }
+    if (!b->devs.empty()) {  // one mark for every target's "written by this run"
+        RunMark *m = mark_new(b->x.device);
+        if (!m) return MTGL_ERR_CUDA;
+        const cudaError_t e = cudaEventRecord(m->ev, b->x.stream);
+        if (e != cudaSuccess) {
+            mark_drop(m);
+            return fail_cuda("cudaEventRecord", e);
+        }
+        for (mtgl_dev *d : b->devs) {
+            if (d->after_batch) mark_drop(d->after_batch);
+            mark_hold(m);
+            d->after_batch = m;
+            d->after_stream = b->x.stream;
+        }
+        mark_drop(m);
     }
     CK(cudaEventRecord(b->done, b->x.stream));
+    return MTGL_OK;
+}
+
+// One mark after the copies queued from contexts' staging areas so far: each area may be
+// rewritten once it has passed.
+int mark_uploads(mtgl_batch *b)
+{
+    if (b->uploaded.empty()) return MTGL_OK;
+    RunMark *m = mark_new(b->x.device);
+    if (!m) return MTGL_ERR_CUDA;
+    const cudaError_t e = cudaEventRecord(m->ev, b->x.stream);
+    if (e != cudaSuccess) {
+        mark_drop(m);
+        return fail_cuda("cudaEventRecord", e);
+    }
+    for (mtgl_dev *d : b->uploaded) d->stage.hold_upload(m);
+    mark_drop(m);
+    b->uploaded.clear();
     return MTGL_OK;
 }
 
@@ -169,6 +228,7 @@ void mtgl_dev_batch_defaults(mtgl_batch_config *cfg)
     cfg->pair_factor = MTGL_TUNED_PAIR_FACTOR;
     cfg->use_graph = 1;
     cfg->order_by_cost = 1;
+    cfg->readback_kernel = 1;
 }
 
 int mtgl_dev_batch_create(const mtgl_batch_config *cfg, mtgl_batch **out)
@@ -189,6 +249,7 @@ int mtgl_dev_batch_create(const mtgl_batch_config *cfg, mtgl_batch **out)
         if (cfg->pair_factor > 0) c.pair_factor = cfg->pair_factor;
         c.use_graph = cfg->use_graph;
         c.order_by_cost = cfg->order_by_cost;
+        c.readback_kernel = cfg->readback_kernel;
     }
     int shift = 0;
     while (shift <= kTileShiftMax && (1 << shift) != c.tile_size) shift++;
@@ -213,6 +274,7 @@ int mtgl_dev_batch_destroy(mtgl_batch *b)
     if (!b) return MTGL_OK;
     cudaSetDevice(b->x.device);
     mtgl_dev_batch_wait(b);
+    mark_uploads(b);  // copies of an open run that never launched: their areas wait on a mark
     cudaStreamSynchronize(b->x.stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
@@ -228,13 +290,14 @@ int mtgl_dev_batch_begin(mtgl_batch *b)
     if (!b) return MTGL_ERR_INVALID;
     CK(cudaSetDevice(b->x.device));
     int st = mtgl_dev_batch_wait(b);
-    if (st || (st = b->stage.wait())) return st;
+    if (st || (st = mark_uploads(b)) || (st = b->stage.wait())) return st;
     b->stage.used = 0;
     b->devs.clear();
     b->sources.clear();
     b->passes.clear();
     b->frames.clear();
     b->readbacks.clear();
+    b->uploaded.clear();
     b->direct_end = 0;
     b->direct_ok = true;
     b->open_tris = 0;
@@ -269,7 +332,9 @@ int involve(mtgl_batch *b, mtgl_dev *d, bool write)
         int st = mtgl_dev_batch_wait(d->batch);
         if (st) return st;
     }
-    if (d->wait_batch) CK(cudaStreamWaitEvent(b->x.stream, d->after_batch, 0));
+    // (a batch that last wrote d on this same stream is ordered before this run already)
+    if (d->after_batch && d->after_stream != b->x.stream)
+        CK(cudaStreamWaitEvent(b->x.stream, d->after_batch->ev, 0));
     b->devs.push_back(d);
     return MTGL_OK;
 }
@@ -315,7 +380,8 @@ int mtgl_dev_batch_add(mtgl_batch *b, mtgl_dev *src, mtgl_dev *target)
         // The batch stream runs this copy after the batch's previous run and before this
         // one; the context's next staging write waits for it.
         CK(cudaMemcpyAsync(b->x.dstage + off, src->stage.p, bytes, cudaMemcpyHostToDevice, b->x.stream));
-        if ((st = src->stage.mark_uploaded(b->x.stream))) return st;
+        src->stage.upload_stream = b->x.stream;  // marked at launch (mark_uploads)
+        b->uploaded.push_back(src);
         b->direct_end = (size_t)off + bytes;
     } else if (bytes) {
         b->direct_ok = false;  // offsets only grow: later passes do not fit either
@@ -346,6 +412,7 @@ int mtgl_dev_batch_launch(mtgl_batch *b)
     CK(cudaSetDevice(b->x.device));
     b->open = false;
     int st;
+    if ((st = mark_uploads(b))) return st;
     if (b->frames.empty()) {
         if (b->readbacks.empty()) return MTGL_OK;
         if ((st = record_after(b))) return st;  // readbacks only

@@ -2,6 +2,7 @@
 // the pass pipeline (dev_pipeline.cu) and the batch executor (dev_batch.cu).
 #pragma once
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -40,6 +41,19 @@ struct PendingDraw {
     int64_t off_pos = -1, off_color = -1, off_tex = -1, off_normal = -1, off_idx = -1, off_vsid = -1;
 };
 
+// An event recorded once at a point of a batch run that many contexts order after (the
+// end of the run's uploads from their staging areas, or the end of the run), held by each
+// of them and returned to a pool when the last lets go: one record per run, not one per
+// context. It is never recorded again while held.
+struct RunMark {
+    cudaEvent_t ev = nullptr;
+    int device = 0;
+    std::atomic<int> refs{0};
+};
+RunMark *mark_new(int device);  // held once, by the caller; null on failure (g_err set)
+void mark_hold(RunMark *m);
+void mark_drop(RunMark *m);
+
 // Pinned host staging. Client data is copied in at enqueue; a flush appends the pass's
 // tables and uploads the whole area with one copy. It is not rewritten while that copy
 // is in flight.
@@ -48,12 +62,17 @@ struct HostStage {
     size_t cap = 0, used = 0;
     cudaEvent_t done = nullptr;  // recorded after the upload that reads the area
     bool inflight = false;
+    // a batch's upload of the area: queued on `upload_stream` and not yet marked (wait
+    // synchronises that stream), then marked by `upload_mark`
+    cudaStream_t upload_stream = nullptr;
+    RunMark *upload_mark = nullptr;
     bool fixed = false;          // refuse to grow (allocation-free flush)
 
     int wait();
     int reserve(size_t bytes, int64_t *off);
     int copy(const void *src, size_t bytes, int64_t *off);
     int mark_uploaded(cudaStream_t s);
+    void hold_upload(RunMark *m);  // the batch upload queued from this area ends at m
     void release();
 };
 
@@ -192,8 +211,8 @@ struct mtgl_dev {
     // stream that a batch must wait for, and a batch this context's stream must wait for
     cudaEvent_t tail = nullptr;
     bool dirty = false;
-    cudaEvent_t after_batch = nullptr;
-    bool wait_batch = false;
+    mtgl::RunMark *after_batch = nullptr;  // end of the last batch run that wrote this context
+    cudaStream_t after_stream = nullptr;   // the stream that run was on
     mtgl_batch *batch = nullptr;  // an unverified batch that writes this context's framebuffer
     std::vector<mtgl_batch *> readers;  // unfinished batches that read this context's resources
 };

@@ -149,4 +149,22 @@ void launch_mip1(const uint32_t *base, int32_t w, int32_t h, uint32_t *mip, cuda
 void launch_draw_pixels(const uint32_t *img, int32_t rx, int32_t ry, int32_t w, int32_t h, const DevRaster *raster,
                         FrameDims dims, uint32_t *color, float *depth, cudaStream_t s);
 
+// Colour read-back by kernel into page-locked host memory mapped into the device's address
+// space (dst is the device-side address): one launch per kReadbackMax items, the items in the
+// launch's parameters. Returns the kernels launched.
+struct ReadbackItem {
+    const uint32_t *src;  // device colour buffer
+    uint32_t *dst;        // device address of the host buffer
+    uint32_t n;           // pixels
+    uint32_t first_unit;  // set by the launcher
+};
+constexpr int kReadbackMax = 128;
+constexpr uint32_t kReadbackUnit = 4096;  // pixels per work unit
+struct ReadbackArgs {
+    ReadbackItem item[kReadbackMax];
+    int32_t count;
+    uint32_t units;
+};
+int launch_readback(const ReadbackItem *items, int n, int sms, cudaStream_t s);
+
 }  // namespace mtgl

@@ -2,6 +2,7 @@
 // staging helpers, scratch, table assembly and the K1 -> K2 -> K3 -> K4 launch sequence.
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <thread>
 
 #include "dev_internal.h"
@@ -18,13 +19,75 @@ int fail_cuda(const char *what, cudaError_t e)
 
 // ------------------------------------------------------------------ host staging
 
+// ------------------------------------------------------------------ run marks
+
+namespace {
+std::mutex g_mark_mu;
+std::vector<RunMark *> g_mark_pool;  // marks no one holds
+}  // namespace
+
+RunMark *mark_new(int device)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_mark_mu);
+        for (size_t i = 0; i < g_mark_pool.size(); i++) {
+            RunMark *m = g_mark_pool[i];
+            if (m->device != device) continue;
+            g_mark_pool[i] = g_mark_pool.back();
+            g_mark_pool.pop_back();
+            m->refs.store(1);
+            return m;
+        }
+    }
+    RunMark *m = new (std::nothrow) RunMark();
+    if (!m) {
+        snprintf(g_err, sizeof(g_err), "out of host memory");
+        return nullptr;
+    }
+    m->device = device;
+    cudaError_t e = cudaEventCreateWithFlags(&m->ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        fail_cuda("cudaEventCreateWithFlags", e);
+        delete m;
+        return nullptr;
+    }
+    m->refs.store(1);
+    return m;
+}
+
+void mark_hold(RunMark *m) { m->refs.fetch_add(1); }
+
+void mark_drop(RunMark *m)
+{
+    if (m->refs.fetch_sub(1) != 1) return;
+    std::lock_guard<std::mutex> lk(g_mark_mu);
+    g_mark_pool.push_back(m);
+}
+
 int HostStage::wait()
 {
     if (inflight) {
         CK(cudaEventSynchronize(done));
         inflight = false;
     }
+    if (upload_stream) {  // a batch upload not marked yet: everything queued on its stream
+        CK(cudaStreamSynchronize(upload_stream));
+        upload_stream = nullptr;
+    }
+    if (upload_mark) {
+        CK(cudaEventSynchronize(upload_mark->ev));
+        mark_drop(upload_mark);
+        upload_mark = nullptr;
+    }
     return MTGL_OK;
+}
+
+void HostStage::hold_upload(RunMark *m)
+{
+    if (upload_mark) mark_drop(upload_mark);
+    mark_hold(m);
+    upload_mark = m;
+    upload_stream = nullptr;
 }
 
 int HostStage::reserve(size_t bytes, int64_t *off)
@@ -102,7 +165,7 @@ int HostStage::mark_uploaded(cudaStream_t s)
 
 void HostStage::release()
 {
-    if (inflight && done) cudaEventSynchronize(done);
+    wait();
     if (p) cudaFreeHost(p);
     if (done) cudaEventDestroy(done);
     p = nullptr;

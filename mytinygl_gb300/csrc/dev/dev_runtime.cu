@@ -244,9 +244,10 @@ int mtgl_dev_enter(mtgl_dev *d)
         int st = mtgl_dev_batch_wait(d->readers.back());
         if (st) return st;
     }
-    if (d->wait_batch) {
-        CK(cudaStreamWaitEvent(d->x.stream, d->after_batch, 0));
-        d->wait_batch = false;
+    if (d->after_batch) {
+        CK(cudaStreamWaitEvent(d->x.stream, d->after_batch->ev, 0));
+        mark_drop(d->after_batch);
+        d->after_batch = nullptr;
     }
     d->dirty = true;
     return MTGL_OK;
@@ -280,7 +281,6 @@ int mtgl_dev_create(int32_t width, int32_t height, mtgl_dev **out)
     cudaStream_t s = d->x.stream;
     CK(cudaEventCreateWithFlags(&d->stage.done, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&d->tail, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&d->after_batch, cudaEventDisableTiming));
     CK(cudaMallocAsync((void **)&d->color, np * 4, s));
     CK(cudaMallocAsync((void **)&d->depth, np * 4, s));
     CK(cudaMallocAsync((void **)&d->stencil, np, s));
@@ -304,7 +304,7 @@ int mtgl_dev_destroy(mtgl_dev *d)
     d->stage.release();
     d->x.destroy();
     cudaEventDestroy(d->tail);
-    cudaEventDestroy(d->after_batch);
+    if (d->after_batch) mark_drop(d->after_batch);
     delete d;
     return MTGL_OK;
 }

@@ -1,4 +1,6 @@
-// k_misc.cu — clears without draws, mip level 1 construction and the glDrawPixels blit.
+// k_misc.cu — clears without draws, mip level 1 construction, the glDrawPixels blit and colour read-back.
+#include <algorithm>
+
 #include "dev_kernels.h"
 
 namespace mtgl {
@@ -96,6 +98,52 @@ void launch_draw_pixels(const uint32_t *img, int32_t rx, int32_t ry, int32_t w, 
     if (w <= 0 || h <= 0) return;
     dim3 grid((w + 255) / 256, h < 65535 ? h : 65535);
     k_draw_pixels<<<grid, 256, 0, s>>>(img, rx, ry, w, h, raster, dims, color, depth);
+}
+
+// Colour read-back into page-locked host memory the device addresses directly: work units
+// of kReadbackUnit pixels over all items of the launch, each block finding its unit's item
+// by binary search over the items' first units; 16-byte copies where both ends allow them.
+__global__ void __launch_bounds__(256) k_readback(const __grid_constant__ ReadbackArgs a)
+{
+    for (uint32_t u = blockIdx.x; u < a.units; u += gridDim.x) {
+        int lo = 0, hi = a.count - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.item[mid].first_unit <= u) lo = mid;
+            else hi = mid - 1;
+        }
+        const ReadbackItem &it = a.item[lo];
+        const uint32_t p0 = (u - it.first_unit) * kReadbackUnit;
+        const uint32_t p1 = min(p0 + kReadbackUnit, it.n);
+        uint32_t v1 = p0;  // end of the 16-byte part
+        if (((reinterpret_cast<uintptr_t>(it.src) | reinterpret_cast<uintptr_t>(it.dst)) & 15u) == 0) {
+            v1 = p0 + ((p1 - p0) & ~3u);
+            for (uint32_t p = p0 + threadIdx.x * 4u; p < v1; p += blockDim.x * 4u)
+                *reinterpret_cast<uint4 *>(it.dst + p) = __ldg(reinterpret_cast<const uint4 *>(it.src + p));
+        }
+        for (uint32_t p = v1 + threadIdx.x; p < p1; p += blockDim.x) it.dst[p] = __ldg(it.src + p);
+    }
+}
+
+int launch_readback(const ReadbackItem *items, int n, int sms, cudaStream_t s)
+{
+    int launches = 0;
+    for (int k = 0; k < n; k += kReadbackMax) {
+        ReadbackArgs a;
+        a.count = std::min(n - k, kReadbackMax);
+        uint32_t units = 0;
+        for (int i = 0; i < a.count; i++) {
+            a.item[i] = items[k + i];
+            a.item[i].first_unit = units;
+            units += (a.item[i].n + kReadbackUnit - 1) / kReadbackUnit;
+        }
+        a.units = units;
+        if (!units) continue;
+        const unsigned grid = std::min<unsigned>(units, (unsigned)std::max(sms, 1) * 8u);
+        k_readback<<<grid, 256, 0, s>>>(a);
+        launches++;
+    }
+    return launches;
 }
 
 }  // namespace mtgl

@@ -331,6 +331,7 @@ int mtgl_server_create(const mtgl_server_config *cfg, mtgl_server **out)
         if (!cfg) {
             s->cfg.batch.use_graph = d.use_graph;
             s->cfg.batch.order_by_cost = d.order_by_cost;
+            s->cfg.batch.readback_kernel = d.readback_kernel;
         }
     }
     s->device = dev_current_device();

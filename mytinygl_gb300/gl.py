@@ -95,7 +95,8 @@ class Stats(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     """mtgl_batch_config (include/mytinygl/mtgl_dev.h); zero fields take the tuned defaults."""
     _fields_ = [("tile_size", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("record_factor", ctypes.c_float),
-                ("pair_factor", ctypes.c_float), ("use_graph", ctypes.c_int32), ("order_by_cost", ctypes.c_int32)]
+                ("pair_factor", ctypes.c_float), ("use_graph", ctypes.c_int32), ("order_by_cost", ctypes.c_int32),
+                ("readback_kernel", ctypes.c_int32)]
 
 
 class BatchStats(ctypes.Structure):

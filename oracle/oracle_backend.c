@@ -1411,6 +1411,7 @@ void mtgl_dev_batch_defaults(mtgl_batch_config *cfg)
     cfg->pair_factor = 8.0f;
     cfg->use_graph = 1;
     cfg->order_by_cost = 1;
+    cfg->readback_kernel = 1;
 }
 
 int mtgl_dev_batch_create(const mtgl_batch_config *cfg, mtgl_batch **out)

@@ -182,3 +182,42 @@ def test_render_read_with_direct_uploads(gpu):
     b.destroy()
     for c in ctxs:
         c.destroy()
+
+
+def test_readback_kernel_destinations(gpu):
+    """Colour read-back into page-locked host memory runs as kernels writing the host buffers
+    (16-byte stores where both ends are aligned, 4-byte ones elsewhere); pageable
+    destinations are copied. Frames with odd sides, a page-locked destination 4 bytes off
+    alignment and pageable ones in one batch: every destination equals the plain path's
+    colour, with read-back kernels on and off, and the kernel mode launches one kernel more
+    than the copy mode for the same run."""
+    torch = pytest.importorskip("torch")
+    scenes = W.uneven_batch(9, seed=21, min_side=17, max_side=131, min_tri=20, max_tri=1500, tex_size=32,
+                            use_vbo=False)
+    want = plain(gpu, scenes)
+    ctxs, streams = setup_frames(gpu, scenes)
+    launches = {}
+    for mode in (1, 0):
+        b = gpu.batch(tile_size=16, readback_kernel=mode)
+        for _ in range(2):
+            keep, hosts = [], []
+            for i, s in enumerate(scenes):
+                n = s.width * s.height
+                if i % 3 == 2:  # pageable
+                    hosts.append(np.zeros((s.height, s.width), np.uint32))
+                    continue
+                off = 1 if i % 3 == 1 else 0  # one word past a 16-byte boundary
+                t = torch.zeros(n + 4, dtype=torch.int32, pin_memory=True)
+                keep.append(t)
+                hosts.append(t.numpy().view(np.uint32)[off:off + n].reshape(s.height, s.width))
+            gpu.play_many(ctxs, streams)
+            b.reset_stats()
+            b.render(ctxs, colors=hosts)
+            b.wait()
+            launches[mode] = b.stats()["kernel_launches"]
+            for h, w, s in zip(hosts, want, scenes):
+                assert np.array_equal(h, w[0]), f"{s.name} (readback_kernel={mode})"
+        b.destroy()
+    assert launches[1] == launches[0] + 1
+    for c in ctxs:
+        c.destroy()

@@ -9,6 +9,10 @@
 namespace mtgl {
 
 constexpr uint32_t kClipClasses = 96;  // one-plane candidates: first plane x in/out pattern; the rest
+// Each class is counted in kClipSlots counters (a block of the count pass uses slot
+// blockIdx % kClipSlots), so that the appends of many blocks do not all meet on a few words.
+constexpr uint32_t kClipSlots = 32;
+constexpr uint32_t kClipBuckets = kClipClasses * kClipSlots;  // class-major
 
 struct GeomArgs {
     const DevDraw *draws;
@@ -29,9 +33,9 @@ struct GeomArgs {
     float *eye_records;               // emit pass output, kEyeWords per record (may be null)
     uint32_t records_cap;             // records the output buffers hold (writes beyond are dropped)
     uint32_t *clip_list;              // triangles that straddle a clip plane (total_tris entries)
-    uint32_t *clip_class;             // per entry: clip class << 24 | rank within the class
+    uint32_t *clip_class;             // per entry: bucket << 20 | rank within the bucket
     uint32_t *clip_sorted;            // the entries grouped by class (null: process clip_list as is)
-    uint32_t *class_count;            // kClipClasses counters (zeroed by the count launch)
+    uint32_t *class_count;            // kClipBuckets counters (zeroed by the count launch)
     uint32_t *clip_count;             // their number (device; zeroed by the count launch)
     int32_t sms;
 };

@@ -461,7 +461,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if ((rc = sc.take(S_TRI_OFFSETS, tris, &tri_offsets))) return rc;
     // clip list, its class words, the class-sorted list and the class counters
     uint32_t *clip_list = nullptr;
-    if ((rc = sc.take(S_CLIP_LIST, 3 * (size_t)tris + kClipClasses, &clip_list))) return rc;
+    if ((rc = sc.take(S_CLIP_LIST, 3 * (size_t)tris + kClipBuckets, &clip_list))) return rc;
     // tile counts, then (persistent ordered launches) the per-tile record-box coverage
     if ((rc = sc.take(S_TILE_COUNT, 2 * ((size_t)ntiles + 1), &tile_count))) return rc;
     // record-box coverage per tile, for the split between tiles run by rounds and per record;
@@ -508,7 +508,8 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ga.tri_offsets = tri_offsets;
     ga.clip_list = clip_list;
     ga.clip_class = clip_list + tris;
-    // sort by class while a class rank fits the class word's 24 bits
+    // sort by class below 2^24 triangles: a bucket then holds under 2^20 entries (its blocks
+    // are every kClipSlots-th of 128 triangles), so a rank fits the class word's 20 bits
     ga.clip_sorted = tris < (1u << 24) ? clip_list + 2 * (size_t)tris : nullptr;
     ga.class_count = clip_list + 3 * (size_t)tris;
     ga.clip_count = x.d_totals + 4;

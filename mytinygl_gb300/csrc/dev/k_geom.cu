@@ -991,11 +991,12 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
         if (lane == first) base = atomicAdd(A.clip_count, (uint32_t)__popc(want));
         base = __shfl_sync(active, base, first);
         uint32_t rank = 0;
+        const uint32_t bucket = cls * kClipSlots + (blockIdx.x & (kClipSlots - 1));
         if (A.clip_sorted) {
-            const uint32_t peers = __match_any_sync(active, straddles ? cls : 0xFFFFFFFFu);
+            const uint32_t peers = __match_any_sync(active, straddles ? bucket : 0xFFFFFFFFu);
             const int leader = __ffs(peers) - 1;
             uint32_t rb = 0;
-            if (straddles && lane == leader) rb = atomicAdd(A.class_count + cls, (uint32_t)__popc(peers));
+            if (straddles && lane == leader) rb = atomicAdd(A.class_count + bucket, (uint32_t)__popc(peers));
             rb = __shfl_sync(active, rb, leader);
             rank = rb + (uint32_t)__popc(peers & below);
         }
@@ -1003,7 +1004,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
             const uint32_t slot = base + (uint32_t)__popc(want & below);
             if (slot < A.total_tris) {
                 A.clip_list[slot] = t;
-                if (A.clip_sorted) A.clip_class[slot] = (cls << 24) | rank;
+                if (A.clip_sorted) A.clip_class[slot] = (bucket << 20) | rank;
             }
             return;
         }
@@ -1057,23 +1058,44 @@ __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
     }
 }
 
-// groups the clip list by class (clip_class): entry i goes to its class's start + its rank
+// groups the clip list by class (clip_class): entry i goes to its bucket's start + its rank
+// (buckets class-major, so each class's entries are contiguous)
 __global__ void __launch_bounds__(256) k_clip_sort(GeomArgs A)
 {
     const uint32_t n = min(*A.clip_count, A.total_tris);
     if (blockIdx.x * blockDim.x >= n) return;  // no entries for this block (uniform)
-    __shared__ uint32_t count[kClipClasses], start[kClipClasses];
-    if (threadIdx.x < kClipClasses) count[threadIdx.x] = A.class_count[threadIdx.x];
+    // exclusive prefix of the bucket counts (class-major), in shared memory: each thread sums
+    // kPer consecutive buckets, the warps scan those sums, then each thread writes its starts
+    constexpr uint32_t kPer = kClipBuckets / 256;
+    static_assert(kClipBuckets % 256 == 0, "buckets per thread");
+    __shared__ uint32_t start[kClipBuckets];
+    __shared__ uint32_t warp_sum[8];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t c[kPer], sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; k++) {
+        c[k] = A.class_count[threadIdx.x * kPer + k];
+        sum += c[k];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sum[warp] = incl;
     __syncthreads();
-    if (threadIdx.x < kClipClasses) {  // exclusive prefix of the class counts, from shared memory
-        uint32_t run = 0;
-        for (uint32_t c = 0; c < threadIdx.x; c++) run += count[c];
-        start[threadIdx.x] = run;
+    uint32_t run = incl - sum;
+    for (uint32_t w = 0; w < warp; w++) run += warp_sum[w];
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; k++) {
+        start[threadIdx.x * kPer + k] = run;
+        run += c[k];
     }
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t w = A.clip_class[i];
-        A.clip_sorted[start[w >> 24] + (w & 0xFFFFFFu)] = A.clip_list[i];
+        A.clip_sorted[start[w >> 20] + (w & 0xFFFFFu)] = A.clip_list[i];
     }
 }
 
@@ -1115,7 +1137,7 @@ int launch_setup_count(const GeomArgs &a, cudaStream_t s)
 {
     if (!a.total_tris) return 0;
     cudaMemsetAsync(a.clip_count, 0, sizeof(uint32_t), s);
-    if (a.clip_sorted) cudaMemsetAsync(a.class_count, 0, kClipClasses * sizeof(uint32_t), s);
+    if (a.clip_sorted) cudaMemsetAsync(a.class_count, 0, kClipBuckets * sizeof(uint32_t), s);
     return launch_setup<false>(a, s);
 }
 

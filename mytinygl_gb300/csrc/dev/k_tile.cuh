@@ -46,6 +46,32 @@ __device__ __forceinline__ float warp_max_depth(float dep, bool in_fb)
 
 constexpr uint32_t kNoPending = 0xFFFFFFFFu;
 
+// Whether a triangle record's coverage test (the three edge functions at integer pixel
+// positions, raster.c:299-302, 534-536) can pass at some pixel of the 8x4 block at (bx, by).
+// Each edge function is affine in the pixel position, so over the block it is largest
+// (smallest, for a negative area) at a corner. The record's positions and per-edge
+// differences are integer-valued floats: when every product the per-pixel test forms over
+// the block is below 2^24 in magnitude, those products are exact and each edge function's
+// sign is the exact one, per pixel and here alike. A block is dropped only then, and only
+// when no pixel of it can pass; otherwise it is kept.
+__device__ __forceinline__ bool block_may_cover(const float4 *q, const float4 &q1, const float4 &q2, int bx, int by)
+{
+    const float area = q2.z;
+    if (!(area > 0.0f) && !(area < 0.0f)) return false;  // zero or NaN area: the test never passes
+    const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
+    const float xl = (float)bx, xh = (float)(bx + 7), yl = (float)by, yh = (float)(by + 3);
+    const bool pos = area > 0.0f;
+    constexpr float kExact = 16777216.0f;  // 2^24
+    // edge function (px - ax) * A - (py - ay) * B
+    auto excludes = [&](float ax, float ay, float A, float B) -> bool {
+        const float pl = (xl - ax) * A, ph = (xh - ax) * A, ql = (yl - ay) * B, qh = (yh - ay) * B;
+        if (!(fabsf(pl) < kExact && fabsf(ph) < kExact && fabsf(ql) < kExact && fabsf(qh) < kExact)) return false;
+        return pos ? fmaxf(pl, ph) - fminf(ql, qh) < 0.0f : fminf(pl, ph) - fmaxf(ql, qh) > 0.0f;
+    };
+    return !(excludes(q0.z, q0.w, q12.y, q12.z) || excludes(q1.x, q1.y, q12.w, q13.x) ||
+             excludes(q0.x, q0.y, q13.y, q13.z));
+}
+
 // The colour stages of a fragment (raster.c:582-705): colour interpolation (or the flat
 // colour), per-fragment lighting, texturing with the alpha test and texture environment,
 // fog. Returns false when the alpha test discards the fragment.
@@ -497,6 +523,8 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                          __float_as_int(bb2.y) < wy0 || __float_as_int(bb.w) > wy0 + 3);
                 flags = __float_as_uint(__ldg(reinterpret_cast<const float *>(q) + R_FLAGS));
                 dmin = __ldg(reinterpret_cast<const float *>(q) + R_DMIN);
+                // a triangle that meets the block's box but none of its pixels is not taken
+                if (take && ((flags >> kRecTypeShift) & 3u) == REC_TRI) take = block_may_cover(q, bb, bb2, wx0, wy0);
             }
             const uint32_t raise_mask = __ballot_sync(0xffffffffu, (flags & kFlagRaisesDepth) != 0);
             const uint32_t zc_l = (flags >> 1) & 3u;

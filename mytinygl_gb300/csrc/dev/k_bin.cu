@@ -132,25 +132,74 @@ __device__ __forceinline__ const DevFrame &rec_tile_box(const float *rec, const 
 
 __device__ __forceinline__ uint32_t records_in(const BinArgs &A) { return min(*A.nrec_dev, A.nrec); }
 
-// tiles per record; records past the real count get 0 so the scan over the capacity is exact
+// The tiles of a record's box that get a pair: every tile for points and lines; for a
+// triangle, the tiles its coverage test can pass in (tri_may_cover_rect over the tile).
+// k_bin_count counts them and k_bin_expand writes them, with this one test.
+struct RecTiles {
+    int tx0, ty0, w, cnt;    // the box in tiles, row-major, cnt tiles
+    bool tri;                // test each tile
+    float4 q0, q1, q2, q12, q13;
+};
+
+__device__ __forceinline__ const DevFrame &rec_tiles_of(const BinArgs &A, uint32_t r, RecTiles &t)
+{
+    const float *rec = A.records + (size_t)r * kRecWords;
+    int tx1, ty1;
+    const DevFrame &F = rec_tile_box(rec, A, t.tx0, t.ty0, tx1, ty1);
+    t.w = tx1 - t.tx0 + 1;
+    t.cnt = t.w * (ty1 - t.ty0 + 1);
+    const float4 *q = reinterpret_cast<const float4 *>(rec);
+    t.q12 = __ldg(q + 12);
+    t.tri = ((__float_as_uint(t.q12.x) >> kRecTypeShift) & 3u) == REC_TRI;
+    if (t.tri) {
+        t.q0 = __ldg(q + 0);
+        t.q1 = __ldg(q + 1);
+        t.q2 = __ldg(q + 2);
+        t.q13 = __ldg(q + 13);
+    }
+    return F;
+}
+
+__device__ __forceinline__ bool tile_gets_pair(const RecTiles &t, int tx, int ty, int sh)
+{
+    if (!t.tri) return true;
+    const float xl = (float)(tx << sh), yl = (float)(ty << sh), e = (float)((1 << sh) - 1);
+    return tri_may_cover_rect(t.q0, t.q1, t.q2, t.q12, t.q13, xl, xl + e, yl, yl + e);
+}
+
+constexpr uint32_t kCountLanes = 8;  // lanes per record in k_bin_count (4 records per warp)
+
+// pairs per record; records past the real count get 0 so the scan over the capacity is exact
 __global__ void __launch_bounds__(256) k_bin_count(BinArgs A)
 {
     const uint32_t n = records_in(A);
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < A.nrec; r += gridDim.x * blockDim.x) {
+    constexpr uint32_t L = kCountLanes, G = 32 / kCountLanes;
+    const uint32_t lane = threadIdx.x & 31u, sub = lane / L, sl = lane % L;
+    const uint32_t gmask = ((1u << L) - 1u) << (sub * L);
+    const uint32_t groups = gridDim.x * (blockDim.x >> 5) * G;
+    for (uint32_t r0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * G; r0 < A.nrec; r0 += groups) {
+        const uint32_t r = r0 + sub;
+        if (r >= A.nrec) continue;
         uint32_t c = 0;
         if (r < n) {
-            int tx0, ty0, tx1, ty1;
-            rec_tile_box(A.records + (size_t)r * kRecWords, A, tx0, ty0, tx1, ty1);
-            c = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+            RecTiles t;
+            rec_tiles_of(A, r, t);
+            if (!t.tri) {
+                c = sl == 0 ? (uint32_t)t.cnt : 0u;
+            } else {
+                for (int i = (int)sl; i < t.cnt; i += (int)L)
+                    c += tile_gets_pair(t, t.tx0 + i % t.w, t.ty0 + i / t.w, A.tile_shift) ? 1u : 0u;
+            }
         }
-        A.rec_tiles[r] = c;
+        c = __reduce_add_sync(gmask, c);
+        if (sl == 0) A.rec_tiles[r] = c;
     }
 }
 
-// A group of L lanes per record (L = 32 / G, G records per warp from the average tiles per
+// A group of L lanes per record (L = 32 / G, G records per warp from the average pairs per
 // record: 1 for large triangles, up to 8 for small ones, so that a warp has several records'
-// loads in flight): the group writes its record's tiles row-major (pairs stay in submission
-// order).
+// loads in flight): the group tests its record's box tiles row-major and writes the pairs of
+// those that get one, in that order (pairs stay in submission order within every tile).
 __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
 {
     const uint32_t n = records_in(A);
@@ -158,26 +207,32 @@ __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
     const uint32_t G = avg >= 32u ? 1u : (avg >= 16u ? 2u : (avg >= 8u ? 4u : 8u));
     const uint32_t L = 32u / G;
     const uint32_t lane = threadIdx.x & 31u, sub = lane / L, sl = lane % L;
+    const uint32_t lmask = L == 32u ? 0xFFFFFFFFu : (1u << L) - 1u;
+    const uint32_t gmask = lmask << (sub * L);
     const uint32_t groups = gridDim.x * (blockDim.x >> 5) * G;
+    const int sh = A.tile_shift;
     for (uint32_t r = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * G + sub; r < n; r += groups) {
-        int tx0, ty0, tx1, ty1;
+        RecTiles t;
+        const DevFrame &F = rec_tiles_of(A, r, t);
         const float *rec = A.records + (size_t)r * kRecWords;
-        const DevFrame &F = rec_tile_box(rec, A, tx0, ty0, tx1, ty1);
         const float4 b1 = __ldg(reinterpret_cast<const float4 *>(rec) + 1);
         const float4 b2 = __ldg(reinterpret_cast<const float4 *>(rec) + 2);
         const int bx0 = __float_as_int(b1.z), by0 = __float_as_int(b1.w);
         const int bx1 = __float_as_int(b2.x), by1 = __float_as_int(b2.y);
-        const int w = tx1 - tx0 + 1;
-        const int cnt = w * (ty1 - ty0 + 1);
         const uint32_t base = A.rec_tiles[r];
-        for (int i = (int)sl; i < cnt; i += (int)L) {
-            if (base + (uint32_t)i >= A.npairs) break;
-            const int tx = tx0 + i % w, ty = ty0 + i / w;
+        uint32_t run = 0;  // pairs of this record written so far
+        for (int i0 = 0; i0 < t.cnt; i0 += (int)L) {
+            const int i = i0 + (int)sl;
+            const int tx = t.tx0 + i % t.w, ty = t.ty0 + i / t.w;
+            const bool get = i < t.cnt && tile_gets_pair(t, tx, ty, sh);
+            const uint32_t m = (__ballot_sync(gmask, get) >> (sub * L)) & lmask;
+            const uint32_t at = base + run + (uint32_t)__popc(m & ((1u << sl) - 1u));
+            run += (uint32_t)__popc(m);
+            if (!get || at >= A.npairs) continue;
             const uint32_t tile = F.tile_base + (uint32_t)(ty * F.dims.tiles_x + tx);
-            A.keys[base + i] = tile;
-            A.vals[base + i] = r;
+            A.keys[at] = tile;
+            A.vals[at] = r;
             if (A.tile_area) {  // pixels of the record's box inside this tile
-                const int sh = A.tile_shift;
                 const int ox = min(bx1, ((tx + 1) << sh) - 1) - max(bx0, tx << sh) + 1;
                 const int oy = min(by1, ((ty + 1) << sh) - 1) - max(by0, ty << sh) + 1;
                 atomicAdd(A.tile_area + tile, (uint32_t)(ox * oy));
@@ -223,7 +278,7 @@ int launch_tile_ranges(const BinArgs &a, cudaStream_t s)
 int launch_bin_count(const BinArgs &a, cudaStream_t s)
 {
     if (!a.nrec) return 0;
-    k_bin_count<<<stride_grid(a.nrec, 256, a.sms), 256, 0, s>>>(a);
+    k_bin_count<<<stride_grid((uint64_t)a.nrec * kCountLanes, 256, a.sms), 256, 0, s>>>(a);
     return 1;
 }
 

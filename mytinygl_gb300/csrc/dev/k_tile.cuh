@@ -46,30 +46,12 @@ __device__ __forceinline__ float warp_max_depth(float dep, bool in_fb)
 
 constexpr uint32_t kNoPending = 0xFFFFFFFFu;
 
-// Whether a triangle record's coverage test (the three edge functions at integer pixel
-// positions, raster.c:299-302, 534-536) can pass at some pixel of the 8x4 block at (bx, by).
-// Each edge function is affine in the pixel position, so over the block it is largest
-// (smallest, for a negative area) at a corner. The record's positions and per-edge
-// differences are integer-valued floats: when every product the per-pixel test forms over
-// the block is below 2^24 in magnitude, those products are exact and each edge function's
-// sign is the exact one, per pixel and here alike. A block is dropped only then, and only
-// when no pixel of it can pass; otherwise it is kept.
+// tri_may_cover_rect over the 8x4 block at (bx, by)
 __device__ __forceinline__ bool block_may_cover(const float4 *q, const float4 &q1, const float4 &q2, int bx, int by)
 {
-    const float area = q2.z;
-    if (!(area > 0.0f) && !(area < 0.0f)) return false;  // zero or NaN area: the test never passes
+    if (!(q2.z > 0.0f) && !(q2.z < 0.0f)) return false;
     const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
-    const float xl = (float)bx, xh = (float)(bx + 7), yl = (float)by, yh = (float)(by + 3);
-    const bool pos = area > 0.0f;
-    constexpr float kExact = 16777216.0f;  // 2^24
-    // edge function (px - ax) * A - (py - ay) * B
-    auto excludes = [&](float ax, float ay, float A, float B) -> bool {
-        const float pl = (xl - ax) * A, ph = (xh - ax) * A, ql = (yl - ay) * B, qh = (yh - ay) * B;
-        if (!(fabsf(pl) < kExact && fabsf(ph) < kExact && fabsf(ql) < kExact && fabsf(qh) < kExact)) return false;
-        return pos ? fmaxf(pl, ph) - fminf(ql, qh) < 0.0f : fminf(pl, ph) - fmaxf(ql, qh) > 0.0f;
-    };
-    return !(excludes(q0.z, q0.w, q12.y, q12.z) || excludes(q1.x, q1.y, q12.w, q13.x) ||
-             excludes(q0.x, q0.y, q13.y, q13.z));
+    return tri_may_cover_rect(q0, q1, q2, q12, q13, (float)bx, (float)(bx + 7), (float)by, (float)(by + 3));
 }
 
 // The colour stages of a fragment (raster.c:582-705): colour interpolation (or the flat

@@ -66,6 +66,34 @@ constexpr int kRecTypeShift = 4;
 constexpr int kRecCtlShift = 8, kRecDepthFuncShift = 20;
 __device__ __forceinline__ uint32_t rec_type(const float *r) { return (__float_as_uint(r[R_FLAGS]) >> kRecTypeShift) & 3u; }
 
+// Whether a triangle record's coverage test (the three edge functions at integer pixel
+// positions, raster.c:299-302, 534-536) can pass at some pixel of the rectangle [xl, xh] x
+// [yl, yh] (integer-valued floats). q0, q1, q2, q12, q13 are the record's 16-byte words 0, 1,
+// 2, 12 and 13. Each edge function is affine in the pixel position, so over the rectangle it
+// is largest (smallest, for a negative area) at a corner. The record's positions and per-edge
+// differences are integer-valued floats: when every product the per-pixel test forms over
+// the rectangle is below 2^24 in magnitude, those products are exact and each edge function's
+// sign is the exact one, per pixel and here alike. The rectangle is ruled out only then, and
+// only when no pixel of it can pass; otherwise it is kept. Binning (per tile) and the tile
+// kernel (per warp block) use this one test.
+__device__ __forceinline__ bool tri_may_cover_rect(const float4 &q0, const float4 &q1, const float4 &q2,
+                                                   const float4 &q12, const float4 &q13, float xl, float xh, float yl,
+                                                   float yh)
+{
+    const float area = q2.z;
+    if (!(area > 0.0f) && !(area < 0.0f)) return false;  // zero or NaN area: the test never passes
+    const bool pos = area > 0.0f;
+    constexpr float kExact = 16777216.0f;  // 2^24
+    // edge function (px - ax) * A - (py - ay) * B
+    auto excludes = [&](float ax, float ay, float A, float B) -> bool {
+        const float pl = (xl - ax) * A, ph = (xh - ax) * A, ql = (yl - ay) * B, qh = (yh - ay) * B;
+        if (!(fabsf(pl) < kExact && fabsf(ph) < kExact && fabsf(ql) < kExact && fabsf(qh) < kExact)) return false;
+        return pos ? fmaxf(pl, ph) - fminf(ql, qh) < 0.0f : fminf(pl, ph) - fmaxf(ql, qh) > 0.0f;
+    };
+    return !(excludes(q0.z, q0.w, q12.y, q12.z) || excludes(q1.x, q1.y, q12.w, q13.x) ||
+             excludes(q0.x, q0.y, q13.y, q13.z));
+}
+
 // Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).
 struct __align__(16) PostVertex {
     float4 clip;

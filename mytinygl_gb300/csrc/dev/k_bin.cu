@@ -133,13 +133,23 @@ __device__ __forceinline__ const DevFrame &rec_tile_box(const float *rec, const 
 __device__ __forceinline__ uint32_t records_in(const BinArgs &A) { return min(*A.nrec_dev, A.nrec); }
 
 // The tiles of a record's box that get a pair: every tile for points and lines; for a
-// triangle, the tiles its coverage test can pass in (tri_may_cover_rect over the tile).
-// k_bin_count counts them and k_bin_expand writes them, with this one test.
+// triangle, the tiles in which its coverage test (edge functions at integer pixel positions,
+// raster.c:299-302, 534-536) can pass. k_bin_count counts them and k_bin_expand writes them,
+// with this one test.
+//
+// The record's positions and per-edge differences are integer-valued floats. When every
+// product (px - ax) * A, (py - ay) * B that the per-pixel test forms over the box's tiles is
+// below 2^24 in magnitude, those products are exact, so each edge function's sign per pixel
+// is the sign of the exact integer. Then each edge's largest value over a tile (a corner:
+// the function is affine) is an int32 stepped per tile column and row, and a tile whose
+// largest value is negative for some edge has no pixel the test passes (for a negative
+// area the signs flip). Otherwise every tile of the box gets a pair.
 struct RecTiles {
-    int tx0, ty0, w, cnt;    // the box in tiles, row-major, cnt tiles
-    bool tri;                // test each tile
-    float4 q0, q1, q2, q12, q13;
+    int tx0, ty0, w, cnt;  // the box in tiles, row-major, cnt tiles
+    int mode;              // kAll, kNone or kTest
+    int e00[3], sx[3], sy[3];  // per edge: value at the first tile's corner, steps per column / row
 };
+constexpr int kAll = 0, kNone = 1, kTest = 2;
 
 __device__ __forceinline__ const DevFrame &rec_tiles_of(const BinArgs &A, uint32_t r, RecTiles &t)
 {
@@ -149,22 +159,49 @@ __device__ __forceinline__ const DevFrame &rec_tiles_of(const BinArgs &A, uint32
     t.w = tx1 - t.tx0 + 1;
     t.cnt = t.w * (ty1 - t.ty0 + 1);
     const float4 *q = reinterpret_cast<const float4 *>(rec);
-    t.q12 = __ldg(q + 12);
-    t.tri = ((__float_as_uint(t.q12.x) >> kRecTypeShift) & 3u) == REC_TRI;
-    if (t.tri) {
-        t.q0 = __ldg(q + 0);
-        t.q1 = __ldg(q + 1);
-        t.q2 = __ldg(q + 2);
-        t.q13 = __ldg(q + 13);
+    const float4 q12 = __ldg(q + 12);
+    t.mode = kAll;
+    if (((__float_as_uint(q12.x) >> kRecTypeShift) & 3u) != REC_TRI) return F;
+    const float4 q0 = __ldg(q + 0), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q13 = __ldg(q + 13);
+    const float area = q2.z;
+    if (!(area > 0.0f) && !(area < 0.0f)) {  // zero or NaN area: the test never passes
+        t.mode = kNone;
+        return F;
     }
+    const int sh = A.tile_shift, ts = 1 << sh;
+    const int xl = t.tx0 << sh, xh = (tx1 << sh) + ts - 1, yl = t.ty0 << sh, yh = (ty1 << sh) + ts - 1;
+    const float ax[3] = {q0.z, q1.x, q0.x}, ay[3] = {q0.w, q1.y, q0.y};
+    const float ea[3] = {q12.y, q12.w, q13.y}, eb[3] = {q12.z, q13.x, q13.z};
+    const bool pos = area > 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        constexpr float kLim = 16777216.0f;  // 2^24
+        if (!(fabsf(ax[k]) < kLim && fabsf(ay[k]) < kLim && fabsf(ea[k]) < kLim && fabsf(eb[k]) < kLim)) return F;
+        const int iax = (int)ax[k], iay = (int)ay[k];
+        const int a = pos ? (int)ea[k] : -(int)ea[k], b = pos ? (int)eb[k] : -(int)eb[k];
+        const long long mx = max(llabs((long long)xl - iax), llabs((long long)xh - iax)) * llabs((long long)a);
+        const long long my = max(llabs((long long)yl - iay), llabs((long long)yh - iay)) * llabs((long long)b);
+        if (mx >= (1ll << 24) || my >= (1ll << 24)) return F;
+        // (x - ax) * a - (y - ay) * b is largest over a tile at x = right edge when a >= 0,
+        // y = top row when b >= 0
+        const int cx = xl + (a >= 0 ? ts - 1 : 0), cy = yl + (b >= 0 ? 0 : ts - 1);
+        t.e00[k] = (cx - iax) * a - (cy - iay) * b;
+        t.sx[k] = a * ts;
+        t.sy[k] = b * ts;
+    }
+    t.mode = kTest;
     return F;
 }
 
-__device__ __forceinline__ bool tile_gets_pair(const RecTiles &t, int tx, int ty, int sh)
+// the i-th tile of the box (row-major) gets a pair
+__device__ __forceinline__ bool tile_gets_pair(const RecTiles &t, int i)
 {
-    if (!t.tri) return true;
-    const float xl = (float)(tx << sh), yl = (float)(ty << sh), e = (float)((1 << sh) - 1);
-    return tri_may_cover_rect(t.q0, t.q1, t.q2, t.q12, t.q13, xl, xl + e, yl, yl + e);
+    if (t.mode != kTest) return t.mode == kAll;
+    const int col = i % t.w, row = i / t.w;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 3; k++) ok = ok && t.e00[k] + col * t.sx[k] - row * t.sy[k] >= 0;
+    return ok;
 }
 
 constexpr uint32_t kCountLanes = 8;  // lanes per record in k_bin_count (4 records per warp)
@@ -184,11 +221,10 @@ __global__ void __launch_bounds__(256) k_bin_count(BinArgs A)
         if (r < n) {
             RecTiles t;
             rec_tiles_of(A, r, t);
-            if (!t.tri) {
+            if (t.mode == kAll) {
                 c = sl == 0 ? (uint32_t)t.cnt : 0u;
-            } else {
-                for (int i = (int)sl; i < t.cnt; i += (int)L)
-                    c += tile_gets_pair(t, t.tx0 + i % t.w, t.ty0 + i / t.w, A.tile_shift) ? 1u : 0u;
+            } else if (t.mode == kTest) {
+                for (int i = (int)sl; i < t.cnt; i += (int)L) c += tile_gets_pair(t, i) ? 1u : 0u;
             }
         }
         c = __reduce_add_sync(gmask, c);
@@ -224,7 +260,7 @@ __global__ void __launch_bounds__(256) k_bin_expand(BinArgs A)
         for (int i0 = 0; i0 < t.cnt; i0 += (int)L) {
             const int i = i0 + (int)sl;
             const int tx = t.tx0 + i % t.w, ty = t.ty0 + i / t.w;
-            const bool get = i < t.cnt && tile_gets_pair(t, tx, ty, sh);
+            const bool get = i < t.cnt && tile_gets_pair(t, i);
             const uint32_t m = (__ballot_sync(gmask, get) >> (sub * L)) & lmask;
             const uint32_t at = base + run + (uint32_t)__popc(m & ((1u << sl) - 1u));
             run += (uint32_t)__popc(m);

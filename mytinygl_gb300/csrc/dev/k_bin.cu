@@ -2,7 +2,8 @@
 //
 // No counterpart in the reference, which scans every triangle's bounding box on one thread
 // (raster.c:532-724). Here each record is expanded into one (tile, record) pair per tile
-// (8, 16 or 32 pixels square) its clamped bounding box touches; pairs are generated in submission order and a
+// (8, 16 or 32 pixels square) of its clamped bounding box in which it can cover a pixel (an
+// exact edge test per tile for triangles); pairs are generated in submission order and a
 // stable LSD radix sort on the tile id (warp match-any ranking plus prefix sums) groups
 // them by tile while keeping that order inside every tile. The tile kernel then walks each
 // list front to back, so blending and stencil updates happen in GL order.

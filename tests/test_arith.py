@@ -1,10 +1,15 @@
-"""Exact-arithmetic checks of the device's division-free byte conversion (CPU only).
+"""Exact-arithmetic checks of the device's shortcuts (CPU only).
 
-The tile kernel converts texel and framebuffer bytes to float as the reference does,
-`(float)v / 255.0f`, but without a division: q = v * r with r = float(1/255), then one
-Markstein correction q' = fma(fma(-q, 255, v), r, q). Here every byte value is checked
-against the correctly rounded quotient with exact rational arithmetic, rounding each
-step to float32 (round to nearest, ties to even) as the GPU's FMA and multiply do.
+Each shortcut must give the reference's result bit for bit:
+- the division-free byte conversion. The tile kernel converts texel and framebuffer bytes to
+  float as the reference does, `(float)v / 255.0f`, but without a division: q = v * r with
+  r = float(1/255), then one Markstein correction q' = fma(fma(-q, 255, v), r, q). Every byte
+  value is checked against the correctly rounded quotient with exact rational arithmetic,
+  rounding each step to float32 (round to nearest, ties to even) as the GPU's FMA and
+  multiply do;
+- the texel wrap shortcuts, the closed form of the line's Bresenham step, level 1 alone at
+  mip weight 1, and small float/int conversions by directed-rounding additions;
+- the exact coverage tests that let binning drop tiles and the tile kernel skip warp blocks.
 """
 from fractions import Fraction as Fr
 
@@ -137,3 +142,119 @@ def test_small_conversions_by_directed_rounding():
         assert s - 3 * 2 ** 22 == np.floor(float(f)), v
     for v in (0, 1, 255, 2 ** 23 - 1):
         assert np.array([0x4B000000 | v], np.uint32).view(np.float32)[0] - np.float32(2 ** 23) == v
+
+
+# ---- exact coverage tests (binning per tile, the tile kernel per 8x4 block)
+
+def _edges(x0, y0, x1, y1, x2, y2):
+    """The record's edges as the tile kernel evaluates them: (ax, ay, A, B) with the edge
+    function (px - ax) * A - (py - ay) * B, all float32 (integer-valued)."""
+    f = np.float32
+    X0, Y0, X1, Y1, X2, Y2 = (f(v) for v in (x0, y0, x1, y1, x2, y2))
+    return [(X1, Y1, Y2 - Y1, X2 - X1), (X2, Y2, Y0 - Y2, X0 - X2), (X0, Y0, Y1 - Y0, X1 - X0)]
+
+
+def _pixel_covered(edges, area, px, py):
+    """The per-pixel coverage test in float32, as shade_pixel forms it."""
+    f = np.float32
+    e = [(f(px) - ax) * A - (f(py) - ay) * B for ax, ay, A, B in edges]
+    return (area > 0 and all(v >= 0 for v in e)) or (area < 0 and all(v <= 0 for v in e))
+
+
+def _rect_excluded_float(edges, area, xl, xh, yl, yh):
+    """tri_may_cover_rect negated (mtgl_device.cuh), in float32."""
+    f = np.float32
+    if not (area > 0 or area < 0):
+        return True
+    lim = f(16777216.0)
+    for ax, ay, A, B in edges:
+        pl, ph = (f(xl) - ax) * A, (f(xh) - ax) * A
+        ql, qh = (f(yl) - ay) * B, (f(yh) - ay) * B
+        if not all(abs(v) < lim for v in (pl, ph, ql, qh)):
+            continue
+        if area > 0 and max(pl, ph) - min(ql, qh) < 0:
+            return True
+        if area < 0 and min(pl, ph) - max(ql, qh) > 0:
+            return True
+    return False
+
+
+def _tile_excluded_int(edges, area, tx0, ty0, tx1, ty1, ts):
+    """The per-tile test of binning (k_bin.cu rec_tiles_of / tile_gets_pair): None when the
+    per-record check fails (every tile kept), else the set of excluded tiles."""
+    xl, xh, yl, yh = tx0 * ts, tx1 * ts + ts - 1, ty0 * ts, ty1 * ts + ts - 1
+    pos = area > 0
+    steps = []
+    for ax, ay, A, B in edges:
+        ax, ay, A, B = int(ax), int(ay), int(A), int(B)
+        a, b = (A, B) if pos else (-A, -B)
+        if max(abs(xl - ax), abs(xh - ax)) * abs(a) >= 1 << 24 or max(abs(yl - ay), abs(yh - ay)) * abs(b) >= 1 << 24:
+            return None
+        cx, cy = xl + (ts - 1 if a >= 0 else 0), yl + (0 if b >= 0 else ts - 1)
+        e00 = (cx - ax) * a - (cy - ay) * b
+        assert -(1 << 31) <= e00 < (1 << 31) and -(1 << 31) <= a * ts < (1 << 31)
+        steps.append((e00, a * ts, b * ts))
+    out = set()
+    for ty in range(ty0, ty1 + 1):
+        for tx in range(tx0, tx1 + 1):
+            col, row = tx - tx0, ty - ty0
+            if not all(e00 + col * sx - row * sy >= 0 for e00, sx, sy in steps):
+                out.add((tx, ty))
+    return out
+
+
+def test_coverage_tests_never_drop_a_covered_pixel():
+    """Random integer triangles (small, large, slivers, both orientations, some far off the
+    pixels so that the exactness check is what decides): every 8x4 block the tile kernel
+    skips and every tile binning drops holds no pixel the per-pixel float32 test covers, and
+    binning's int32 stepped values agree with the float corner test wherever both apply."""
+    rng = np.random.default_rng(7)
+    ts = 16
+    checked = dropped_blocks = dropped_tiles = 0
+    for k in range(1500):
+        scale = [6, 40, 300][k % 3]
+        off = 0 if k % 7 else int(rng.integers(-3_000_000, 3_000_000))
+        cx, cy = int(rng.integers(0, 200)), int(rng.integers(0, 200))
+        xs = [cx + int(v) for v in rng.integers(-scale, scale + 1, 3)]
+        ys = [cy + int(v) for v in rng.integers(-scale, scale + 1, 3)]
+        if k % 11 == 0:
+            xs[2] = xs[0] + (xs[1] - xs[0]) // 2 + 1  # near-degenerate sliver
+        xs[0] += off
+        f = np.float32
+        area = (f(xs[2]) - f(xs[0])) * (f(ys[1]) - f(ys[0])) - (f(ys[2]) - f(ys[0])) * (f(xs[1]) - f(xs[0]))
+        if abs(area) < 0.5:
+            continue
+        edges = _edges(xs[0], ys[0], xs[1], ys[1], xs[2], ys[2])
+        minx, maxx = max(min(xs), 0), min(max(xs), 255)
+        miny, maxy = max(min(ys), 0), min(max(ys), 255)
+        if minx > maxx or miny > maxy:
+            continue
+        # the per-pixel float32 test over the box, vectorised (same operations, same order)
+        gx, gy = np.meshgrid(np.arange(minx, maxx + 1, dtype=np.float32), np.arange(miny, maxy + 1, dtype=np.float32))
+        e = [(gx - ax) * A - (gy - ay) * B for ax, ay, A, B in edges]
+        cov = (e[0] >= 0) & (e[1] >= 0) & (e[2] >= 0) if area > 0 else (e[0] <= 0) & (e[1] <= 0) & (e[2] <= 0)
+
+        def any_covered(x0_, x1_, y0_, y1_):
+            x0_, y0_ = max(x0_, minx), max(y0_, miny)
+            x1_, y1_ = min(x1_, maxx), min(y1_, maxy)
+            return x0_ <= x1_ and y0_ <= y1_ and bool(cov[y0_ - miny:y1_ - miny + 1, x0_ - minx:x1_ - minx + 1].any())
+
+        assert _pixel_covered(edges, area, int(gx.flat[0]), int(gy.flat[0])) == bool(cov.flat[0])
+        for by in range(miny - miny % 4, maxy + 1, 4):
+            for bx in range(minx - minx % 8, maxx + 1, 8):
+                if _rect_excluded_float(edges, area, bx, bx + 7, by, by + 3):
+                    dropped_blocks += 1
+                    assert not any_covered(bx, bx + 7, by, by + 3), (k, bx, by)
+        tx0, ty0, tx1, ty1 = minx // ts, miny // ts, maxx // ts, maxy // ts
+        ex = _tile_excluded_int(edges, area, tx0, ty0, tx1, ty1, ts)
+        if ex is None:
+            continue
+        for tx, ty in ex:
+            dropped_tiles += 1
+            assert not any_covered(tx * ts, tx * ts + ts - 1, ty * ts, ty * ts + ts - 1), (k, tx, ty)
+        for ty in range(ty0, ty1 + 1):
+            for tx in range(tx0, tx1 + 1):
+                fl = _rect_excluded_float(edges, area, tx * ts, tx * ts + ts - 1, ty * ts, ty * ts + ts - 1)
+                assert fl == ((tx, ty) in ex), (k, tx, ty)
+                checked += 1
+    assert dropped_blocks > 2000 and dropped_tiles > 400 and checked > 4000

@@ -18,8 +18,8 @@ Lines printed (one JSON object each, rank 0 only):
                frames); L2 is flushed (a 256 MiB write on that stream) before every step.
   e2e          the same frames through the public C ABI with host inputs (client vertex
                arrays copied host->device every step) and every colour buffer read back,
-               timed on the host clock; for the batch, with two steps in flight (two sets
-               of contexts alternating) and, as `sequential_value`, one at a time.
+               timed on the host clock; for the batch, with three steps in flight (three
+               sets of contexts taking turns) and, as `sequential_value`, one at a time.
   roofline     the tile raster/ROP kernel (K4): compulsory bytes per launch over its mean
                launch time (CUDA events inside the library), against the measured HBM copy peak.
   cpu_baseline the CPU oracle (a restatement of MyTinyGL's renderer) on all host cores, one

@@ -73,7 +73,9 @@ int mtgl_batch_render(mtgl_batch *b, GLState *const *ctxs, int32_t n);
 /* mtgl_batch_render, then after the run a copy of each context's colour buffer (width*height
  * packed RGBA8, row 0 = top) into colors[i]; NULL entries (or a NULL colors) copy nothing.
  * The copies have landed when mtgl_dev_batch_wait returns; page-locked destinations keep
- * them asynchronous. */
+ * them asynchronous. Each colors[i] must hold the frame's width * height pixels: those in
+ * page-locked memory the device maps are written by a read-back kernel (one launch per 128
+ * frames) unless mtgl_batch_config.readback_kernel is 0, the others are copied. */
 int mtgl_batch_render_read(mtgl_batch *b, GLState *const *ctxs, uint32_t *const *colors, int32_t n);
 
 /* Replay a GL command stream onto ctx (made current). No counterpart in the reference.
@@ -86,10 +88,10 @@ int mtgl_batch_render_read(mtgl_batch *b, GLState *const *ctxs, uint32_t *const 
 int mtgl_play(GLState *ctx, const void *stream, size_t bytes);
 /* mtgl_play for each (ctxs[i], streams[i]). When the contexts are distinct and in no
  * unfinished batch, the streams play concurrently on a pool of host threads
- * (MTGL_PLAY_THREADS, default: the online cores), each context on one thread; otherwise in
- * order on the calling thread. Every
- * stream is played; returns the status of the first failing stream by index. The calling
- * thread's current context is restored. */
+ * (MTGL_PLAY_THREADS, default: the online cores), each context on one thread, the longest
+ * streams claimed first; otherwise in order on the calling thread. Every stream is played;
+ * returns the status of the first failing stream by index. The calling thread's current
+ * context is restored. */
 int mtgl_play_many(GLState *const *ctxs, const void *const *streams, const size_t *bytes, int32_t n);
 /* number of entry points a stream can call (the function-id range) */
 int mtgl_play_function_count(void);

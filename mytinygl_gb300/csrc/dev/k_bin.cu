@@ -151,6 +151,7 @@ struct RecTiles {
     int e00[3], sx[3], sy[3];  // per edge: value at the first tile's corner, steps per column / row
 };
 constexpr int kAll = 0, kNone = 1, kTest = 2;
+constexpr int kTestMinTiles = 4;  // smaller boxes keep every tile: little to drop, and the set-up dominates
 
 __device__ __forceinline__ const DevFrame &rec_tiles_of(const BinArgs &A, uint32_t r, RecTiles &t)
 {
@@ -160,8 +161,9 @@ __device__ __forceinline__ const DevFrame &rec_tiles_of(const BinArgs &A, uint32
     t.w = tx1 - t.tx0 + 1;
     t.cnt = t.w * (ty1 - t.ty0 + 1);
     const float4 *q = reinterpret_cast<const float4 *>(rec);
-    const float4 q12 = __ldg(q + 12);
     t.mode = kAll;
+    if (t.cnt < kTestMinTiles) return F;
+    const float4 q12 = __ldg(q + 12);
     if (((__float_as_uint(q12.x) >> kRecTypeShift) & 3u) != REC_TRI) return F;
     const float4 q0 = __ldg(q + 0), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q13 = __ldg(q + 13);
     const float area = q2.z;

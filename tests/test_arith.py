@@ -182,6 +182,8 @@ def _rect_excluded_float(edges, area, xl, xh, yl, yh):
 def _tile_excluded_int(edges, area, tx0, ty0, tx1, ty1, ts):
     """The per-tile test of binning (k_bin.cu rec_tiles_of / tile_gets_pair): None when the
     per-record check fails (every tile kept), else the set of excluded tiles."""
+    if (tx1 - tx0 + 1) * (ty1 - ty0 + 1) < 4:  # kTestMinTiles: small boxes keep every tile
+        return None
     xl, xh, yl, yh = tx0 * ts, tx1 * ts + ts - 1, ty0 * ts, ty1 * ts + ts - 1
     pos = area > 0
     steps = []

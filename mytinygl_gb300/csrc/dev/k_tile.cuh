@@ -3,12 +3,12 @@
 //
 // A CTA owns one tile (8, 16 or 32 pixels square) at a time; thread t owns one pixel for
 // the whole pass, so the pixel's colour, depth and stencil stay in registers between
-// triangles. Each warp covers an 8x4 block of the tile. The CTA walks the tile's record
-// list (submission order, built by the binning pass) in chunks staged through shared
-// memory; every thread runs the reference's fragment pipeline for its own pixel: edge
-// functions at the integer pixel position, barycentrics, stencil test/ops, depth test,
-// colour (flat / smooth / per-fragment lighting), texture with alpha test and texenv, fog,
-// depth write, blend, masked write. Because a pixel is only ever touched by its own thread,
+// triangles. Each warp covers an 8x4 block of the tile and walks the tile's record list
+// (submission order, built by the binning pass) on its own, 32 records per step, taking
+// those whose exact edge test can pass in its block. Every thread runs the reference's
+// fragment pipeline for its own pixel: edge functions at the integer pixel position,
+// barycentrics, stencil test/ops, depth test, colour (flat / smooth / per-fragment
+// lighting), texture with alpha test and texenv, fog, depth write, blend, masked write. Because a pixel is only ever touched by its own thread,
 // in-order blending and stencil updates need no atomics. Clears of the pass are applied
 // first; a clear that covers the whole tile means that buffer is never read from memory.
 //

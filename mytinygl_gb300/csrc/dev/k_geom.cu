@@ -8,6 +8,9 @@
 // culling (raster.c:751-774, 901-958) and the per-triangle part of
 // rasterize_triangle_smooth (raster.c:458-529). The count pass sizes the output; after an
 // exclusive scan the emit pass writes each record at its submission-order position.
+// Triangles that straddle a clip plane leave k_setup for a list, grouped by clip class
+// (k_clip_sort) and clipped by k_clip: one crossed plane in registers, anything else by
+// Sutherland-Hodgman in local memory; their records land at the same positions.
 #include <algorithm>
 
 #include "dev_kernels.h"

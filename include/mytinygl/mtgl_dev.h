@@ -148,6 +148,8 @@ typedef struct {
     uint64_t draws, input_triangles, setup_triangles, bin_entries, fragments;
     uint64_t passes, kernel_launches;
     uint64_t staged_bytes;         /* client data (attributes, indices, state ids) staged */
+    uint64_t allocations;          /* device or page-locked allocations made for this context's
+                                      passes (scratch, staging areas) */
 } mtgl_stats;
 
 /* Device time per pipeline phase, summed over the passes since profiling was enabled

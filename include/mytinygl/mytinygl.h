@@ -59,9 +59,14 @@ int mtgl_set_option(GLState *ctx, int option, int value);
  * comes from one static 64 MiB device array that every GPU loading the library holds.
  * Returns 0, or MTGL_ERR_OVERFLOW when the pass needs more scratch than that or more
  * staging than ctx already holds; the pass then stays queued and renders at the next
- * mtgl_finish. All calls share the array: calls whose GPU work overlaps (contexts on
- * different threads) race and must be serialised. The first call on a device looks up
- * the array's address; make it before any stream capture. */
+ * mtgl_finish. All calls share the array, so calls whose GPU work overlapped would race:
+ * every context renders on its own stream, so that holds even for two contexts flushed
+ * one after the other from one thread. The library therefore orders them: each call's
+ * GPU work waits for the previous call's on the same device (one event per device,
+ * under a lock), so they run in the order the host made them, whatever the context or
+ * thread. Work the caller enqueues on mtgl_cuda_stream outside these calls is not
+ * ordered against them. The first call on a device looks up the array's address and
+ * creates that event; make it before any stream capture. */
 int mtgl_flush_noalloc(GLState *ctx);
 
 /* Render the pending frame (clears, then draws) of each of ctxs[0..n) in one batch; see

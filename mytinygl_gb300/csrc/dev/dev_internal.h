@@ -67,6 +67,7 @@ struct HostStage {
     cudaStream_t upload_stream = nullptr;
     RunMark *upload_mark = nullptr;
     bool fixed = false;          // refuse to grow (allocation-free flush)
+    uint64_t allocs = 0;         // page-locked allocations made by growth
 
     int wait();
     int reserve(size_t bytes, int64_t *off);
@@ -116,6 +117,7 @@ struct PoolScratch final : ScratchSource {
     cudaStream_t stream = nullptr;
     void *p[kScratchSlots] = {};
     size_t cap[kScratchSlots] = {};
+    uint64_t allocs = 0;  // device allocations made by growth
     int get(int slot, size_t bytes, void **out) override;
     void release();
 };
@@ -129,6 +131,7 @@ struct Exec {
     PoolScratch pool;
     uint8_t *dstage = nullptr;
     size_t dcap = 0;
+    uint64_t allocs = 0;  // device allocations of the staging copy
     uint32_t *d_totals = nullptr;  // [0] records, [1] pairs, [2] tiles' records, [3] sort scratch, [4] clip list
     uint32_t *h_totals = nullptr;  // pinned copy of [0..1]
     unsigned long long *d_frags = nullptr;
@@ -206,6 +209,7 @@ struct mtgl_dev {
     mtgl::HostStage stage;
     mtgl::Pass pass;
     mtgl_stats stats{};
+    uint64_t alloc_base = 0;  // allocation count at the last reset of the counters
     bool depth_rejection = true;
     // ordering against batches, which run on their own streams: work of this context's
     // stream that a batch must wait for, and a batch this context's stream must wait for

@@ -104,6 +104,7 @@ int HostStage::reserve(size_t bytes, int64_t *off)
         ncap = std::max(ncap, (size_t)1 << 20);
         uint8_t *n = nullptr;
         CK(cudaMallocHost((void **)&n, ncap));
+        allocs++;
         if (used) memcpy(n, p, used);
         if (p) cudaFreeHost(p);
         p = n;
@@ -195,6 +196,7 @@ int PoolScratch::get(int slot, size_t bytes, void **out)
         p[slot] = nullptr;
         cap[slot] = 0;
         CK(cudaMallocAsync(&p[slot], ncap, stream));
+        allocs++;
         cap[slot] = ncap;
     }
     *out = p[slot];
@@ -266,6 +268,7 @@ int Exec::ensure_dstage(size_t bytes, bool may_grow, size_t keep)
     const size_t cap = std::max(bytes, dcap * 2);
     uint8_t *n = nullptr;
     CK(cudaMallocAsync((void **)&n, cap, stream));
+    allocs++;
     if (dstage && keep) CK(cudaMemcpyAsync(n, dstage, std::min(keep, dcap), cudaMemcpyDeviceToDevice, stream));
     if (dstage) CK(cudaFreeAsync(dstage, stream));
     dstage = n;

@@ -595,6 +595,7 @@ int mtgl_dev_stats(mtgl_dev *d, mtgl_stats *out)
     CK(cudaMemcpy(&f, d->x.d_frags, sizeof(f), cudaMemcpyDeviceToHost));
     *out = d->stats;
     out->fragments = f;
+    out->allocations = d->x.pool.allocs + d->x.allocs + d->stage.allocs - d->alloc_base;
     return MTGL_OK;
 }
 
@@ -638,6 +639,7 @@ int mtgl_dev_reset_stats(mtgl_dev *d)
     int st = mtgl_dev_finish(d);
     if (st) return st;
     memset(&d->stats, 0, sizeof(d->stats));
+    d->alloc_base = d->x.pool.allocs + d->x.allocs + d->stage.allocs;
     CK(cudaMemsetAsync(d->x.d_frags, 0, sizeof(unsigned long long), d->x.stream));
     CK(cudaStreamSynchronize(d->x.stream));
     return MTGL_OK;
@@ -661,10 +663,13 @@ int mtgl_dev_reset_stats(mtgl_dev *d)
 // anything is drawn, and stays queued (mtgl_finish or mtgl_dev_flush can still render
 // it). The pass's tables must fit the staging areas the context already holds. Every
 // call, from every context on the device, shares the one array and overwrites what the
-// previous call left; calls whose work overlaps on the GPU (two contexts on different
-// streams) race, so callers serialise them. The array's device address is looked up
-// once per device, on the first call with that device current; make that first call
-// before any stream capture.
+// previous call left. Two calls whose GPU work overlapped would race on it (each context
+// has its own stream, so even two calls made one after the other from one thread would),
+// so each call's work waits on the GPU for the previous call's: one event per device,
+// recorded at the end of every call and waited on by the next, under a lock, so calls
+// run on the GPU in the order the host made them. The array's device address and the
+// event are set up once per device, on the first call with that device current; make
+// that first call before any stream capture.
 // ============================================================================================
 #include <mutex>
 
@@ -675,33 +680,49 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_noalloc_mu;
-uint8_t *g_noalloc_addr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mu;  // held for a whole call: set-up, and the wait - launch - record sequence
+struct NoAllocDevice {
+    uint8_t *scratch = nullptr;  // device address of g_noalloc_scratch
+    cudaEvent_t done = nullptr;  // end of the last call's GPU work on this device
+    bool pending = false;        // `done` has been recorded
+};
+NoAllocDevice g_noalloc[kNoAllocMaxDevices];
 
-// set-up, once per device with that device current: host code needs the array's device address
-int noalloc_scratch(int device, uint8_t **out)
+// set-up, once per device with that device current: host code needs the array's device
+// address, and the calls need their ordering event; the caller holds g_noalloc_mu
+int noalloc_setup(int device, NoAllocDevice **out)
 {
     if (device < 0 || device >= kNoAllocMaxDevices) {
         snprintf(g_err, sizeof(g_err), "mtgl_flush_noalloc: device %d out of range", device);
         return MTGL_ERR_INVALID;
     }
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[device]) {
+    NoAllocDevice &nd = g_noalloc[device];
+    if (!nd.scratch) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return fail_cuda("cudaGetSymbolAddress(g_noalloc_scratch)", e);
-        g_noalloc_addr[device] = static_cast<uint8_t *>(p);
+        if (!nd.done && (e = cudaEventCreateWithFlags(&nd.done, cudaEventDisableTiming)) != cudaSuccess)
+            return fail_cuda("cudaEventCreateWithFlags", e);
+        nd.scratch = static_cast<uint8_t *>(p);
     }
-    *out = g_noalloc_addr[device];
+    *out = &nd;
     return MTGL_OK;
 }
 
-// bump allocator over the static array (256-byte aligned pieces)
+// Bump allocator over the static array (256-byte aligned pieces). A slot taken again gets
+// its previous piece back when the new size fits in it, so re-taking a slot (the scan
+// temporaries are taken once per sort pass) costs no space.
 struct Carve final : ScratchSource {
     uint8_t *base = nullptr;
     size_t used = 0, cap = 0;
-    int get(int, size_t bytes, void **out) override
+    size_t at_of[kScratchSlots] = {}, len_of[kScratchSlots] = {};
+    bool held[kScratchSlots] = {};
+    int get(int slot, size_t bytes, void **out) override
     {
+        if (slot >= 0 && slot < kScratchSlots && held[slot] && bytes <= len_of[slot]) {
+            *out = base + at_of[slot];
+            return MTGL_OK;
+        }
         const size_t at = (used + 255) & ~(size_t)255;
         if (at + bytes > cap) {
             snprintf(g_err, sizeof(g_err),
@@ -711,10 +732,25 @@ struct Carve final : ScratchSource {
             return MTGL_ERR_OVERFLOW;
         }
         used = at + bytes;
+        if (slot >= 0 && slot < kScratchSlots) {
+            held[slot] = true;
+            at_of[slot] = at;
+            len_of[slot] = bytes;
+        }
         *out = base + at;
         return MTGL_OK;
     }
 };
+
+// A refused pass may have recorded some of its profiling events: drop them, so the next
+// pass's five events are read as one group.
+void drop_profile_marks(Exec &x, size_t keep)
+{
+    while (x.ev_pending.size() > keep) {
+        x.ev_pool.push_back(x.ev_pending.back());
+        x.ev_pending.pop_back();
+    }
+}
 
 int flush_pass_noalloc(mtgl_dev *d)
 {
@@ -722,10 +758,14 @@ int flush_pass_noalloc(mtgl_dev *d)
     if (st) return st;
     Pass &P = d->pass;
     if (P.draws.empty()) return run_clears_only(d);  // clears launch kernels only
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice *nd = nullptr;
+    if ((st = noalloc_setup(d->device, &nd))) return st;
     Carve cv;
-    if ((st = noalloc_scratch(d->device, &cv.base))) return st;
+    cv.base = nd->scratch;
     cv.cap = kNoAllocScratchBytes;
     const size_t used0 = d->stage.used;
+    const size_t marks0 = d->x.ev_pending.size();
     FrameSrc fs{d, &P, 0};
     Tables t;
     d->stage.fixed = true;  // tables go into the staging areas the context already holds
@@ -737,10 +777,17 @@ int flush_pass_noalloc(mtgl_dev *d)
                      "mtgl_flush_noalloc: the pass's tables exceed the context's staging areas; the pass stays queued");
         return st;
     }
+    // the previous call's kernels (any context, any stream) are done with the array first
+    if (nd->pending) CK(cudaStreamWaitEvent(d->x.stream, nd->done, 0));
     PipeConfig c = plain_config(d, t);
     PipeOut o;
-    if ((st = run_pipeline(d->x, cv, d->stage, t, c, &o))) {
+    st = run_pipeline(d->x, cv, d->stage, t, c, &o);
+    // whatever this call enqueued, the next call waits for it
+    CK(cudaEventRecord(nd->done, d->x.stream));
+    nd->pending = true;
+    if (st) {
         d->stage.used = used0;  // drop the tables; the pass stays queued
+        drop_profile_marks(d->x, marks0);
         return st;
     }
     if ((st = d->stage.mark_uploaded(d->x.stream))) return st;

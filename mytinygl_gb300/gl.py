@@ -89,7 +89,8 @@ def _nbytes(x):
 class Stats(ctypes.Structure):
     """mtgl_stats (include/mytinygl/mtgl_dev.h)"""
     _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "input_triangles", "setup_triangles", "bin_entries",
-                                               "fragments", "passes", "kernel_launches", "staged_bytes")]
+                                               "fragments", "passes", "kernel_launches", "staged_bytes",
+                                               "allocations")]
 
 
 class BatchConfig(ctypes.Structure):

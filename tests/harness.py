@@ -19,7 +19,6 @@ REPO = os.path.dirname(TESTS)
 ORACLE_DIR = os.path.join(REPO, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libmtgl_oracle.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libmtgl_ref.so")
-REF_SRC = "/root/reference"
 GOLDEN_DIR = os.path.join(TESTS, "golden")
 
 
@@ -28,11 +27,22 @@ def oracle():
     return G.load(ORACLE_LIB)
 
 
+def reference_root():
+    """The reference checkout's root directory, or None where its sources are not present
+    (oracle/Makefile knows where to look; MTGL_REF_SRC overrides it)."""
+    r = subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref-dir"], capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 and r.stdout.strip() else None
+
+
+def has_reference_sources():
+    return reference_root() is not None
+
+
 def reference():
     """The reference build, or None where its sources are not present."""
-    if not os.path.isdir(os.path.join(REF_SRC, "src")):
+    if not has_reference_sources():
         return None
-    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref", f"REF={REF_SRC}"], check=True, capture_output=True)
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref"], check=True, capture_output=True)
     return G.load(REF_LIB)
 
 

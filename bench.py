@@ -199,6 +199,111 @@ def scene_bytes(scene, start):
     return total
 
 
+PARITY_TOLERANCE = "depth and stencil bit-exact (NaN payloads aside), RGBA8 colour within 1 LSB per channel"
+
+
+def frame_buffers(scene):
+    """Buffers the frame part of a scene clears (a frame played again on a context leaves only
+    these defined as the frame alone would)."""
+    bits = 0
+    for name, a in scene.cmds[W.frame_start(scene):]:
+        if name == "glClear":
+            bits |= int(a[0])
+    return {"color": bool(bits & G.GL_COLOR_BUFFER_BIT), "depth": bool(bits & G.GL_DEPTH_BUFFER_BIT),
+            "stencil": bool(bits & G.GL_STENCIL_BUFFER_BIT)}
+
+
+class Parity:
+    """Oracle-versus-GPU statistics over many frames: colour max error and mismatching-pixel
+    fraction, depth and stencil mismatches, glGetError agreement."""
+
+    def __init__(self):
+        self.lock = threading.Lock()
+        self.frames = self.pixels = self.color_px = self.color_bad = 0
+        self.color_max = 0
+        self.depth_bad = self.stencil_bad = self.error_bad = 0
+        self.buffers = set()
+        self.worst = None
+
+    def add(self, want, got, buffers, name=""):
+        """want/got: (colour u32, depth f32 or None, stencil u8 or None, gl error or None)."""
+        cmax = cbad = dbad = sbad = 0
+        npx = int(want[0].size)
+        if buffers.get("color") and want[0] is not None and got[0] is not None:
+            a = want[0].view(np.uint8).reshape(*want[0].shape, 4).astype(np.int16)
+            b = got[0].view(np.uint8).reshape(*got[0].shape, 4).astype(np.int16)
+            d = np.abs(a - b).max(axis=-1)
+            cmax = int(d.max()) if d.size else 0
+            cbad = int((d > 0).sum())
+        if buffers.get("depth") and want[1] is not None and got[1] is not None:
+            same = (want[1].view(np.uint32) == got[1].view(np.uint32)) | (np.isnan(want[1]) & np.isnan(got[1]))
+            dbad = int((~same).sum())
+        if buffers.get("stencil") and want[2] is not None and got[2] is not None:
+            sbad = int((want[2] != got[2]).sum())
+        with self.lock:
+            self.frames += 1
+            self.pixels += npx
+            self.buffers |= {k for k, v in buffers.items() if v}
+            if buffers.get("color"):
+                self.color_px += npx
+            self.color_bad += cbad
+            if cmax > self.color_max:
+                self.worst = name
+            self.color_max = max(self.color_max, cmax)
+            self.depth_bad += dbad
+            self.stencil_bad += sbad
+            if want[3] is not None and got[3] is not None and int(want[3]) != int(got[3]):
+                self.error_bad += 1
+
+    def summary(self):
+        ok = (self.color_max <= 1 and self.depth_bad == 0 and self.stencil_bad == 0 and self.error_bad == 0
+              and self.frames > 0)
+        return {"frames_compared": self.frames, "pixels_compared": self.pixels,
+                "buffers": sorted(self.buffers), "color_max_err": self.color_max,
+                "color_mismatch_frac": round(self.color_bad / max(1, self.color_px), 9),
+                "depth_mismatches": self.depth_bad, "stencil_mismatches": self.stencil_bad,
+                "gl_error_mismatches": self.error_bad, "worst_color_frame": self.worst,
+                "tolerance": PARITY_TOLERANCE, "pass": ok,
+                "against": "CPU oracle (restatement of MyTinyGL's renderer, pinned bit-exact to the reference "
+                           "build and its golden fixtures), same seeded inputs"}
+
+
+def gpu_frame(ctx, buffers=None):
+    c, d, s = ctx.read()
+    return c, d, s, ctx.glGetError()
+
+
+def oracle_frame(lib, scene):
+    c = lib.context(scene.width, scene.height)
+    try:
+        scene.play(c)
+        col, dep, st = c.read()
+        return col, dep, st, c.glGetError()
+    finally:
+        c.destroy()
+
+
+def oracle_parity(scenes, gpu_frames, threads=None):
+    """Each scene rendered whole on the CPU oracle (one context per thread) and compared with the
+    GPU's frame of it. Untimed: this is the checker, not the baseline."""
+    lib = _oracle_lib()
+    threads = threads or os.cpu_count() or 1
+    par = Parity()
+    t0 = time.perf_counter()
+
+    def one(i):
+        par.add(oracle_frame(lib, scenes[i]), gpu_frames[i], frame_buffers(scenes[i]), scenes[i].name)
+
+    # largest frames first, so the threads finish together
+    order = sorted(range(len(scenes)), key=lambda i: -W.scene_triangles(scenes[i]) - scenes[i].width * scenes[i].height)
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, order))
+    out = par.summary()
+    out["oracle_wall_s"] = round(time.perf_counter() - t0, 2)
+    return out
+
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -281,6 +386,7 @@ def run_ours(args, spec):
     ctx.glib.lib.mtgl_set_profiling(ctx.handle, 0)
     fps = job_rate(args.steps, total_ms / 1e3)
     tested_per_frame = st["fragments"] / args.steps
+    gpu_out = gpu_frame(ctx) if not args.no_parity else None  # the last timed frame
     ctx.destroy()
     frags_per_frame = covered_fragments(lib, scene, fs)
 
@@ -331,11 +437,8 @@ def run_ours(args, spec):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded; mytinygl_gb300/workloads.py)",
-        "config": {"workload": spec["name"], "description": spec["desc"], "width": scene.width,
-                   "height": scene.height, "input_triangles": int(st["input_triangles"] / args.steps),
-                   "setup_triangles": int(rec), "bin_entries": int(pairs), "tile": 16,
-                   "l2": "flushed before every timed frame (256 MiB write on the renderer's stream)",
-                   "parallelism": f"replicas x{world}"},
+        "config": single_config(spec, scene, world),
+        "pipeline": {"setup_triangles": int(rec), "bin_entries": int(pairs), "tile": 16},
         "fragments_per_s": round(frags_per_frame * fps, 1),
         "fragments_per_frame": int(frags_per_frame),
         "depth_tested_fragments_per_frame": int(tested_per_frame),
@@ -358,9 +461,34 @@ def run_ours(args, spec):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(spec, args.cpu_seconds)
+    if rank == 0 and gpu_out is not None:
+        out["parity"] = oracle_parity([scene], [gpu_out])
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
+
+
+L2_NOTE = "GPU arm: L2 flushed before every timed step (256 MiB write on the rendering stream)"
+
+
+def single_config(spec, scene, world):
+    """The workload keys of a single-frame line (the same in both arms)."""
+    return {"workload": spec["name"], "description": spec["desc"], "width": scene.width, "height": scene.height,
+            "input_triangles": W.scene_triangles(scene), "l2": L2_NOTE, "parallelism": f"replicas x{world}"}
+
+
+def batch_config(spec, scenes, world):
+    return {"workload": spec["name"] if len(scenes) == 256 else f"uneven_batch_{len(scenes)}_frames",
+            "description": spec["desc"], "frames_per_step": len(scenes),
+            "pixels_per_step": sum(sc.width * sc.height for sc in scenes),
+            "input_triangles_per_step": sum(W.scene_triangles(sc) for sc in scenes), "l2": L2_NOTE,
+            "parallelism": f"replicas x{world}"}
+
+
+def serve_config(spec, args, requests, world):
+    return {"workload": spec["name"], "description": spec["desc"], "offered_rate": 2000.0,
+            "duration_s": args.serve_seconds, "requests": requests, "memory_budget_gib": 40,
+            "parallelism": f"replicas x{world}"}
 
 
 def tex_bytes_of(scene):
@@ -437,6 +565,8 @@ def run_batch(args, spec):
     total_ms = sum(s_.elapsed_time(e) for s_, e in zip(starts, ends))
     bst = batch.stats()
     fps = job_rate(args.steps * BATCH_FRAMES, total_ms / 1e3)
+    # the frames of the last timed step, for the parity check against the oracle
+    gpu_frames = [gpu_frame(c) for c in ctxs] if not args.no_parity else None
 
     # host clock, outside the clock sampler (its NVML queries stall the driver): the batched
     # path and the plain per-frame path (each frame's pass flushed on its own context, as
@@ -555,15 +685,11 @@ def run_batch(args, spec):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded; mytinygl_gb300/workloads.py uneven_batch)",
-        "config": {"workload": spec["name"] if BATCH_FRAMES == 256 else f"uneven_batch_{BATCH_FRAMES}_frames",
-                   "description": spec["desc"], "frames_per_step": BATCH_FRAMES,
-                   "pixels_per_step": npix, "input_triangles_per_step": tris,
-                   "setup_triangles_per_step": int(rec), "bin_entries_per_step": int(pairs),
-                   "tile": bst["tile_size"], "persistent_ctas": bst["ctas"],
-                   "record_capacity": bst["record_capacity"], "pair_capacity": bst["pair_capacity"],
-                   "graph_replays": bst["graph_replays"], "graph_captures": bst["graph_captures"],
-                   "l2": "flushed before every timed step (256 MiB write on the batch stream)",
-                   "parallelism": f"replicas x{world}"},
+        "config": batch_config(spec, scenes, world),
+        "pipeline": {"setup_triangles_per_step": int(rec), "bin_entries_per_step": int(pairs),
+                     "tile": bst["tile_size"], "persistent_ctas": bst["ctas"],
+                     "record_capacity": bst["record_capacity"], "pair_capacity": bst["pair_capacity"],
+                     "graph_replays": bst["graph_replays"], "graph_captures": bst["graph_captures"]},
         "batched_wall_frames_per_s": round(batched_wall_fps, 2),
         "plain_wall_frames_per_s": round(plain_best, 2),
         "plain_wall_frames_per_s_by_sync": {k: round(v, 2) for k, v in plain_fps.items()},
@@ -589,6 +715,8 @@ def run_batch(args, spec):
     }
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_batch_baseline(args.cpu_seconds)
+    if rank == 0 and gpu_frames is not None:
+        out["parity"] = oracle_parity(scenes, gpu_frames)
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
@@ -682,6 +810,19 @@ def run_serve(args, spec):
     ereqs = _serve_requests(etrace, srv.now() + 0.05, out_for)
     srv.run_trace(ereqs)
     esumm = _latency_summary(ereqs)
+
+    # parity: a seeded sample of the timed trace's requests, served again as one burst with
+    # their colour read back, against the oracle rendering the same calls
+    psample = []
+    if not args.no_parity:
+        pick = np.random.default_rng(61).choice(len(trace), size=min(SERVE_PARITY_REQUESTS, len(trace)),
+                                                replace=False)
+        psample = [trace[int(i)] for i in sorted(pick)]
+        pouts = [np.zeros((h, w), np.uint32) for _, _, w, h, _ in psample]
+        preqs = _serve_requests([(0.0,) + tuple(r[1:]) for r in psample], srv.now() + 0.01,
+                                lambda i, w, h: pouts[i].ctypes.data)
+        srv.run_trace(preqs)
+        pfailed = sum(1 for r in preqs if r.status != 0)
     e2e_fps = job_rate(esumm["completed"], esumm["span_s"])
     d2h = sum(w * h * 4 for _, _, w, h, _ in etrace) / max(1, len(etrace))
     srv.destroy()
@@ -692,9 +833,8 @@ def run_serve(args, spec):
         "steps": len(reqs), "warmup": args.warmup, "ms_per_step": summ["mean_ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; mytinygl_gb300/workloads.py serve_scenes / serve_trace)",
-        "config": {"workload": spec["name"], "description": spec["desc"], "offered_rate": rate,
-                   "duration_s": args.serve_seconds, "requests": len(reqs), "executors": 2, "max_batch": 64,
-                   "memory_budget_gib": 40, "parallelism": f"replicas x{world}"},
+        "config": serve_config(spec, args, len(reqs), world),
+        "pipeline": {"executors": 2, "max_batch": 64},
         "latency_ms": {"p50": summ["p50_ms"], "p99": summ["p99_ms"], "mean": summ["mean_ms"],
                        "max": summ["max_ms"]},
         "served": summ, "batches": batches,
@@ -708,16 +848,68 @@ def run_serve(args, spec):
                 "d2h_bytes_per_step": int(d2h), "latency_ms": {"p50": esumm["p50_ms"], "p99": esumm["p99_ms"]}},
         "gpu_launches": int(st1["kernel_launches"] - st0["kernel_launches"]), "clocks": clocks.summary(),
     }
+    if rank == 0 and psample:
+        out["parity"] = serve_parity(scenes, psample, pouts)
+        out["parity"]["gpu_failed_requests"] = pfailed
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         times = cpu_serve_sample(_oracle_lib(), args.cpu_seconds, threads)
+        times1 = cpu_serve_sample(_oracle_lib(), min(args.cpu_seconds, 10.0), 1)
+        times_s = cpu_serve_sample(_oracle_lib(shipped=True), args.cpu_seconds, threads)
         out["cpu_baseline"] = {"value": round(threads / statistics.mean(times), 4), "unit": "frames/s",
-                               "cores": threads, "kind": "port",
+                               "cores": threads, "kind": "port", "cpu_model": cpu_model(), "build": STRICT_BUILD,
                                "sample": (f"{len(times)} requests of the trace, each frame on its own oracle "
-                                          f"context, {threads} threads; frames/s = threads / mean frame time")}
+                                          f"context, {threads} threads; frames/s = threads / mean frame time"),
+                               "one_thread": {"value": round(1.0 / statistics.mean(times1), 4), "unit": "frames/s",
+                                              "cores": 1, "sample": f"{len(times1)} requests of the trace in order"},
+                               "shipped_flags": {"value": round(threads / statistics.mean(times_s), 4),
+                                                 "unit": "frames/s", "cores": threads, "build": SHIPPED_BUILD,
+                                                 "sample": f"{len(times_s)} requests of the trace in order"},
+                               "vs_reference": PORT_VS_REFERENCE}
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
+
+
+SERVE_PARITY_REQUESTS = 16
+
+
+def serve_oracle_frame(lib, scene, w, h, mv):
+    """A serving request rendered on the oracle: the scene's resident part on a context of the
+    request's size, then the request's viewport and modelview, then the frame part."""
+    c = lib.context(w, h)
+    try:
+        k = W.frame_start(scene)
+        scene.play(c, 0, k)
+        c.glViewport(0, 0, w, h)
+        c.glMatrixMode(G.GL_MODELVIEW)
+        c.glLoadMatrixf(np.asarray(mv, np.float32))
+        scene.play(c, k)
+        col, _, _ = c.read(depth=False, stencil=False)
+        return col, None, None, None
+    finally:
+        c.destroy()
+
+
+def serve_parity(scenes, sample, colours):
+    """Served colour of each sampled request against the oracle (the server reads back colour
+    only). Untimed checker."""
+    lib = _oracle_lib()
+    par = Parity()
+    t0 = time.perf_counter()
+
+    def one(i):
+        _, sc, w, h, mv = sample[i]
+        par.add(serve_oracle_frame(lib, scenes[sc], w, h, mv), (colours[i], None, None, None), {"color": True},
+                f"scene{sc}_{w}x{h}")
+
+    order = sorted(range(len(sample)), key=lambda i: -W.scene_triangles(scenes[sample[i][1]]))
+    with cf.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        list(ex.map(one, order))
+    out = par.summary()
+    out["oracle_wall_s"] = round(time.perf_counter() - t0, 2)
+    out["sample"] = f"{len(sample)} requests of the timed trace (seeded choice), served again as one burst"
+    return out
 
 
 def cpu_serve_sample(lib, seconds, threads):
@@ -781,81 +973,142 @@ def cpu_batch_sample(seconds):
 
 
 def cpu_batch_baseline(seconds):
+    """The oracle on all host cores (one context per frame and thread) over whole frames of the
+    batch, plus the same on one thread (every 8th frame of the sample) and with the
+    reference's shipped optimisation flags."""
     lib = _oracle_lib()
     sample, k, threads = cpu_batch_sample(seconds)
     wall = cpu_batch_frames(lib, sample, threads)
+    one = sample[::8]
+    wall1 = cpu_batch_frames(lib, one, 1)
+    wall_s = cpu_batch_frames(_oracle_lib(shipped=True), sample, threads)
     return {"value": round(len(sample) / wall, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(), "build": STRICT_BUILD,
             "sample": (f"every {k}th frame of the 256-frame batch ({len(sample)} frames, whole frames), "
-                       f"one oracle context per frame on {threads} threads"), "wall_s": round(wall, 2)}
+                       f"one oracle context per frame on {threads} threads"), "wall_s": round(wall, 2),
+            "one_thread": {"value": round(len(one) / wall1, 4), "unit": "frames/s", "cores": 1,
+                           "sample": f"{len(one)} whole frames (every 8th of the sample) on one thread"},
+            "shipped_flags": {"value": round(len(sample) / wall_s, 4), "unit": "frames/s", "cores": threads,
+                              "build": SHIPPED_BUILD, "sample": "the same frames and threads"},
+            "vs_reference": PORT_VS_REFERENCE}
 
 
-def _oracle_lib():
-    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True, capture_output=True)
-    return G.load(os.path.join(REPO, "oracle", "_build", "libmtgl_oracle.so"))
+STRICT_BUILD = "oracle (restatement of MyTinyGL's renderer), -O2 -ffp-contract=off"
+SHIPPED_BUILD = "oracle with MyTinyGL's shipped flags (Makefile:3) minus -march=native: -O3 -ffast-math"
+PORT_VS_REFERENCE = ("oracle frame time / reference frame time, same frames, one thread, measured where the "
+                     "reference's sources compile (oracle/speed_vs_reference.py): 1.09-1.26 strict, "
+                     "1.05-1.52 with shipped flags")
 
 
-def cpu_frame_time(lib, spec, ntri, reps):
-    scene = spec["builder"](use_vbo=False, ntri=ntri) if spec["name"] != WORKLOADS["sphere"]["name"] else \
-        spec["builder"](use_vbo=False)
+def cpu_model():
+    """The host CPU's model name (lscpu), for the baseline lines."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def _oracle_lib(shipped=False):
+    """The CPU oracle (checker and CPU baseline); shipped=True: the build with the reference's
+    shipped optimisation flags, for timing only."""
+    target, name = ("shipped", "libmtgl_oracle_shipped.so") if shipped else ("all", "libmtgl_oracle.so")
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), target], check=True, capture_output=True)
+    return G.load(os.path.join(REPO, "oracle", "_build", name))
+
+
+def cpu_frame_time(lib, scene, reps):
+    """Seconds per whole frame (the frame part; the resident part is played once, untimed)."""
     fs = W.frame_start(scene)
     ctx = lib.context(scene.width, scene.height)
     scene.play(ctx, 0, fs)
     t0 = time.perf_counter()
     for _ in range(reps):
         scene.play(ctx, fs)
+    ctx.glFinish()
     dt = time.perf_counter() - t0
     ctx.destroy()
     return dt / reps
 
 
+def cpu_single_frames(lib, scene, reps, threads):
+    """Frames/s of `threads` contexts each rendering the whole frame `reps` times at once."""
+    with cf.ThreadPoolExecutor(threads) as ex:
+        times = list(ex.map(lambda _: cpu_frame_time(lib, scene, reps), range(threads)))
+    return threads / statistics.median(times)
+
+
+def single_reps(lib, spec, scene, seconds):
+    """Renders per context so that each thread works about `seconds` (at least one whole frame),
+    from a 500-triangle cut's time scaled to the full count."""
+    full = spec["full_tris"]
+    cut = spec["builder"](use_vbo=False, ntri=min(full, 500)) if spec is not WORKLOADS["sphere"] else scene
+    t = cpu_frame_time(lib, cut, 1) * (full / min(full, 500) if spec is not WORKLOADS["sphere"] else 1.0)
+    return max(1, int(seconds / max(t, 1e-6)))
+
+
 def cpu_baseline(spec, seconds):
     """The oracle on every host core, one context per thread (the reference keeps one current
-    context per thread, gl_api.c:14-23), each rendering a sample of the frame's triangles."""
+    context per thread, gl_api.c:14-23), each rendering the whole frame; plus one thread, and
+    the build with the reference's shipped flags."""
     lib = _oracle_lib()
     threads = os.cpu_count() or 1
-    full = spec["full_tris"]
-    sample = min(full, 500)
-    t1 = cpu_frame_time(lib, spec, sample, 1)
-    per_tri = t1 / sample
-    # about `seconds` of work per thread in total, at least one render each
-    sample = int(min(full, max(100, (seconds / 3.0) / max(per_tri, 1e-9))))
-    reps = 3 if sample < full else max(1, int(seconds / max(t1 * full / 500, 1e-6)))
+    scene = spec["builder"](use_vbo=False)
+    reps = single_reps(lib, spec, scene, seconds)
     t0 = time.perf_counter()
-    with cf.ThreadPoolExecutor(threads) as ex:
-        times = list(ex.map(lambda _: cpu_frame_time(lib, spec, sample, reps), range(threads)))
+    fps = cpu_single_frames(lib, scene, reps, threads)
     wall = time.perf_counter() - t0
-    frame_s = statistics.median(times) * (full / sample)
-    return {"value": round(threads / frame_s, 5), "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": (f"first {sample} of {full} triangles of the same frame, {reps} renders per context, "
-                       f"{threads} contexts on {threads} threads; frame time scaled by {full}/{sample}"),
-            "wall_s": round(wall, 2)}
+    fps1 = cpu_single_frames(lib, scene, reps, 1)
+    fps_s = cpu_single_frames(_oracle_lib(shipped=True), scene, reps, threads)
+    return {"value": round(fps, 5), "unit": "frames/s", "cores": threads, "kind": "port", "cpu_model": cpu_model(),
+            "build": STRICT_BUILD,
+            "sample": (f"the whole frame, {reps} renders per context, {threads} contexts on {threads} threads"),
+            "wall_s": round(wall, 2),
+            "one_thread": {"value": round(fps1, 5), "unit": "frames/s", "cores": 1,
+                           "sample": f"the whole frame, {reps} renders on one thread"},
+            "shipped_flags": {"value": round(fps_s, 5), "unit": "frames/s", "cores": threads,
+                              "build": SHIPPED_BUILD, "sample": "the same renders and threads"},
+            "vs_reference": PORT_VS_REFERENCE}
 
 
 def run_reference(args, spec):
+    """The reference arm: the CPU implementation of the path (the oracle, built with MyTinyGL's
+    shipped optimisation flags) on every host core, one context per thread, on the same
+    workload and config as the GPU arm; rank 0 only."""
     world, rank, local = dist_init()
     if rank != 0:
         return None
-    lib = _oracle_lib()
+    lib = _oracle_lib(shipped=True)
+    threads = os.cpu_count() or 1
+    common = {"impl": "reference", "metric": "frames/s", "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+              "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+              "dtype": "f32"}
+
+    def line(fps, ms, config, data, desc, **extra):
+        out = dict(common, value=round(fps, 5), ms_per_step=round(ms, 3), data=data, config=config)
+        out.update(extra)
+        out["cpu_baseline"] = {"value": round(fps, 5), "unit": "frames/s", "cores": threads, "kind": "port",
+                               "build": SHIPPED_BUILD, "cpu_model": cpu_model(), "sample": desc,
+                               "vs_reference": PORT_VS_REFERENCE}
+        out["e2e"] = {"value": round(fps, 5), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+        return out
+
     if spec is WORKLOADS["serve"]:
-        threads = os.cpu_count() or 1
         budget = 120.0 / max(1, args.steps + args.warmup)
         cpu_serve_sample(lib, min(2.0, budget), threads)  # warm-up
         times = cpu_serve_sample(lib, budget * (args.steps / max(1, args.steps)), threads)
         fps = threads / statistics.mean(times)
         desc = (f"{len(times)} requests of the trace in order, each frame rendered on its own oracle context "
                 f"(scene set-up untimed), {threads} threads at once; frames/s = threads / mean frame time")
-        return {"impl": "reference", "metric": "frames/s", "value": round(fps, 4), "unit": "frames/s",
-                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": round(statistics.mean(times) * 1e3, 3), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded; mytinygl_gb300/workloads.py serve_scenes / serve_trace)",
-                "config": {"workload": spec["name"], "description": spec["desc"]},
-                "latency_ms": {"p50": round(float(np.percentile(times, 50)) * 1e3, 3),
-                               "p99": round(float(np.percentile(times, 99)) * 1e3, 3)},
-                "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": threads, "kind": "port",
-                                 "sample": desc},
-                "e2e": {"value": round(fps, 4), "unit": "frames/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
+        return line(fps, statistics.mean(times) * 1e3,
+                    serve_config(spec, args, len(W.serve_trace(args.serve_seconds, 2000.0, seed=6)), world),
+                    "synthetic (seeded; mytinygl_gb300/workloads.py serve_scenes / serve_trace)", desc,
+                    latency_ms={"p50": round(float(np.percentile(times, 50)) * 1e3, 3),
+                                "p99": round(float(np.percentile(times, 99)) * 1e3, 3)})
     if spec is WORKLOADS["batch"]:
         sample, k, threads = cpu_batch_sample(120.0 / max(1, args.steps + args.warmup))
         for _ in range(args.warmup):
@@ -864,24 +1117,23 @@ def run_reference(args, spec):
         fps = len(sample) / statistics.median(walls)
         desc = (f"every {k}th frame of the 256-frame batch ({len(sample)} whole frames) per step, one oracle "
                 f"context per frame on {threads} threads")
-        return {"impl": "reference", "metric": "frames/s", "value": round(fps, 5), "unit": "frames/s",
-                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": round(statistics.median(walls) * 1e3, 3), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded; mytinygl_gb300/workloads.py uneven_batch)",
-                "config": {"workload": spec["name"], "description": spec["desc"]},
-                "cpu_baseline": {"value": round(fps, 5), "unit": "frames/s", "cores": threads, "kind": "port",
-                                 "sample": desc},
-                "e2e": {"value": round(fps, 5), "unit": "frames/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-    threads = os.cpu_count() or 1
+        return line(fps, statistics.median(walls) * 1e3, batch_config(spec, W.uneven_batch(BATCH_FRAMES, use_vbo=False), world),
+                    "synthetic (seeded; mytinygl_gb300/workloads.py uneven_batch)", desc)
+    # single frames: a frame's first `sample` triangles per context and step, the frame time
+    # scaled to the full triangle count, so the whole run stays within a couple of minutes
     full = spec["full_tris"]
-    sample = min(full, 500)
-    t1 = cpu_frame_time(lib, spec, sample, 1)
-    budget = 120.0 / max(1, args.steps + args.warmup)  # whole run within a couple of minutes
-    sample = int(min(full, max(100, budget / max(t1 / sample, 1e-9))))
-    step = lambda: list(cf.ThreadPoolExecutor(threads).map(lambda _: cpu_frame_time(lib, spec, sample, 1),
-                                                           range(threads)))
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    if spec is WORKLOADS["sphere"]:
+        sample, scene = full, spec["builder"](use_vbo=False)
+    else:
+        t1 = cpu_frame_time(lib, spec["builder"](use_vbo=False, ntri=500), 1)
+        sample = int(min(full, max(100, budget * 500 / max(t1, 1e-9))))
+        scene = spec["builder"](use_vbo=False, ntri=sample)
+
+    def step():
+        with cf.ThreadPoolExecutor(threads) as ex:
+            return list(ex.map(lambda _: cpu_frame_time(lib, scene, 1), range(threads)))
+
     for _ in range(args.warmup):
         step()
     per = []
@@ -889,18 +1141,11 @@ def run_reference(args, spec):
     for _ in range(args.steps):
         per.append(statistics.median(step()))
     wall = time.perf_counter() - t0
-    frame_s = statistics.median(per) * (full / sample)
-    fps = threads / frame_s
+    fps = threads / (statistics.median(per) * (full / sample))
     desc = (f"first {sample} of {full} triangles of the frame per context, {threads} contexts on {threads} "
             f"threads per step; frame time scaled by {full}/{sample}")
-    return {"impl": "reference", "metric": "frames/s", "value": round(fps, 5), "unit": "frames/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(wall * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; mytinygl_gb300/workloads.py)",
-            "config": {"workload": spec["name"], "description": spec["desc"]},
-            "cpu_baseline": {"value": round(fps, 5), "unit": "frames/s", "cores": threads, "kind": "port",
-                             "sample": desc},
-            "e2e": {"value": round(fps, 5), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line(fps, wall * 1e3 / args.steps, single_config(spec, spec["builder"](use_vbo=False), world),
+                "synthetic (seeded; mytinygl_gb300/workloads.py)", desc)
 
 
 def main():
@@ -912,6 +1157,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batch")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline work per thread")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle comparison of the timed frames")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving trace length (workload serve)")
     ap.add_argument("--frames", type=int, default=256, help="frames per step of the batch workload")
     args = ap.parse_args()

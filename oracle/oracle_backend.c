@@ -693,6 +693,17 @@ static void raster_smooth(mtgl_dev *dv, int32_t x0, int32_t y0, float z0, float 
         }
     }
     float fx0 = (float)x0, fy0 = (float)y0, fx1 = (float)x1, fy1 = (float)y1, fx2 = (float)x2, fy2 = (float)y2;
+    /* the state the loop reads, held in locals: the framebuffer stores below may alias the
+       state block's integer fields as far as the compiler knows */
+    const int depth_test = rs->depth_test, depth_write = rs->depth_test && rs->depth_mask;
+    const uint32_t depth_func = rs->depth_func;
+    const int stencil = rs->stencil_test, blend = rs->blend, fog = rs->fog, flat = rs->shade_model == GL_FLAT;
+    const int lit_frag = rs->lighting && (rs->shade_model == GL_PHONG || (back && rs->lit.two_side));
+    const int all_mask = rs->color_mask[0] && rs->color_mask[1] && rs->color_mask[2] && rs->color_mask[3];
+    uint32_t *const color = dv->color;
+    float *const depthbuf = dv->depth;
+    const int32_t fbw = dv->w;
+    uint64_t frags = 0;
     for (int32_t y = minY; y <= maxY; y++) {
         for (int32_t x = minX; x <= maxX; x++) {
             float px = (float)x, py = (float)y;
@@ -701,30 +712,32 @@ static void raster_smooth(mtgl_dev *dv, int32_t x0, int32_t y0, float z0, float 
             float e2 = edge_fn(fx0, fy0, fx1, fy1, px, py);
             if (!((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) || (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0)))
                 continue;
-            dv->stats.fragments++;
+            frags++;
+            /* (x, y) lies inside the framebuffer: the box was clamped to it above */
+            const size_t pi = (size_t)y * fbw + x;
             float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
             float z = b0 * z0 + b1 * z1 + b2 * z2;
             float depth = map_depth(rs, z);
             uint8_t sv = 0;
-            if (rs->stencil_test) {
+            if (stencil) {
                 sv = get_stencil(dv, x, y);
                 if (!stencil_test(rs->stencil_func, rs->stencil_ref, rs->stencil_mask, sv)) {
                     write_stencil_masked(dv, x, y, stencil_op(rs->stencil_fail, sv, rs->stencil_ref), rs->stencil_writemask);
                     continue;
                 }
             }
-            if (rs->depth_test) {
-                if (!cmp_test(rs->depth_func, depth, get_depth(dv, x, y))) {
-                    if (rs->stencil_test)
+            if (depth_test) {
+                if (!cmp_test(depth_func, depth, depthbuf[pi])) {
+                    if (stencil)
                         write_stencil_masked(dv, x, y, stencil_op(rs->stencil_zfail, sv, rs->stencil_ref),
                                              rs->stencil_writemask);
                     continue;
                 }
             }
-            if (rs->stencil_test)
+            if (stencil)
                 write_stencil_masked(dv, x, y, stencil_op(rs->stencil_zpass, sv, rs->stencil_ref), rs->stencil_writemask);
-            col c = (rs->shade_model == GL_FLAT) ? c2 : c_bary(c0, c1, c2, b0, b1, b2);
-            if (rs->lighting) {
+            col c = flat ? c2 : c_bary(c0, c1, c2, b0, b1, b2);
+            if (lit_frag) {
                 if (rs->shade_model == GL_PHONG) {
                     v3 ep = v3_bary(ep0, ep1, ep2, b0, b1, b2);
                     v3 en = v3_bary(en0, en1, en2, b0, b1, b2);
@@ -734,7 +747,7 @@ static void raster_smooth(mtgl_dev *dv, int32_t x0, int32_t y0, float z0, float 
                         mat = &rs->lit.back;
                     }
                     c = compute_lighting(&rs->lit, ep, en, mat);
-                } else if (back && rs->lit.two_side) {
+                } else {
                     v3 ep = v3_bary(ep0, ep1, ep2, b0, b1, b2);
                     v3 en = v3_scale(v3_bary(en0, en1, en2, b0, b1, b2), -1.0f);
                     c = compute_lighting(&rs->lit, ep, en, &rs->lit.back);
@@ -768,13 +781,15 @@ static void raster_smooth(mtgl_dev *dv, int32_t x0, int32_t y0, float z0, float 
                 default: c = c_mul(c, tc); break;
                 }
             }
-            if (rs->fog) c = apply_fog(rs, c, b0 * ez0 + b1 * ez1 + b2 * ez2, 1);
-            if (rs->depth_test && rs->depth_mask) put_depth(dv, x, y, depth);
-            if (rs->blend) c = blend_colors(rs, c, c_from_rgba32(get_pixel(dv, x, y)));
+            if (fog) c = apply_fog(rs, c, b0 * ez0 + b1 * ez1 + b2 * ez2, 1);
+            if (depth_write) depthbuf[pi] = depth;
+            if (blend) c = blend_colors(rs, c, c_from_rgba32(color[pi]));
             c = c_clamp(c);
-            write_pixel_masked(dv, x, y, c);
+            if (all_mask) color[pi] = c_to_rgba32(c);
+            else write_pixel_masked(dv, x, y, c);
         }
     }
+    dv->stats.fragments += frags;
 }
 
 /* ------------------------------------------------------------------ lines and points */

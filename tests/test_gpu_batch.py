@@ -6,6 +6,9 @@ against the plain per-context GPU path bit for bit. Covers every tile size, grap
 and replay, the cost-ordered work queue, the capacity-overflow re-run, frames that flush
 passes of their own before the batch, and contexts reused after a batch.
 """
+import concurrent.futures as cf
+import os
+
 import numpy as np
 import pytest
 
@@ -221,3 +224,32 @@ def test_readback_kernel_destinations(gpu):
     assert launches[1] == launches[0] + 1
     for c in ctxs:
         c.destroy()
+
+
+@pytest.mark.slow
+def test_full_uneven_batch_matches_oracle(gpu, oracle):
+    """All 256 frames of the benchmark's uneven batch (sides 64-1024, 100-200k triangles, seed
+    3) rendered by one mtgl_batch_render with the tuned defaults, each against the oracle
+    rendering the same frame alone: depth and stencil exact, colour within 1 LSB."""
+    scenes = W.uneven_batch(256)
+    ctxs, streams = setup_frames(gpu, scenes)
+    b = gpu.batch()
+    for _ in range(2):  # the second run replays the captured graph
+        gpu.play_many(ctxs, streams)
+        b.render(ctxs)
+    b.wait()
+    got = read_all(ctxs)
+    b.destroy()
+    for c in ctxs:
+        c.destroy()
+
+    def check(i):
+        s = scenes[i]
+        stats = harness.compare(render(oracle, s), got[i], harness.cleared_buffers(s))
+        harness.assert_parity(stats, color_tol=1, name=s.name)
+        return stats["color_max_err"]
+
+    order = sorted(range(len(scenes)), key=lambda i: -W.scene_triangles(scenes[i]))
+    with cf.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        errs = list(ex.map(check, order))
+    assert len(errs) == 256 and max(errs) <= 1

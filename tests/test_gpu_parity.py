@@ -61,6 +61,20 @@ def test_rop_reduced(gpu, oracle):
     check(gpu, oracle, W.rop_scene(480, 270, ntri=60000))
 
 
+@pytest.mark.slow
+def test_textured_full_size(gpu, oracle):
+    """The benchmark's textured frame at its real size: 1920x1080, 100k clip-straddling
+    triangles, 512^2 trilinear texture, 8 point lights, EXP fog (seed 1)."""
+    check(gpu, oracle, W.textured_scene())
+
+
+@pytest.mark.slow
+def test_rop_full_size(gpu, oracle):
+    """The benchmark's ROP frame at its real size: 1920x1080, 1M small triangles blended in
+    submission order, alpha test, stencil INCR, depth LEQUAL without writes (seed 2)."""
+    check(gpu, oracle, W.rop_scene())
+
+
 def test_immediate_equals_arrays(gpu):
     """The same triangles through glBegin/glEnd and through glDrawArrays give the same image."""
     rng = np.random.default_rng(9)

@@ -98,13 +98,45 @@ def test_served_frames_match_oracle(gpu, oracle, scenes):
 
 
 def test_alone_equals_in_the_mix(gpu, scenes):
+    """Every request of a loaded trace, served again alone, gives the same frame bit for bit."""
     trace = W.serve_trace(0.03, 3000.0, nscenes=len(scenes), seed=23, resolutions=RES)
     _, mixed, _ = serve(gpu, scenes, trace, executors=3, max_batch=6)
-    for i in (0, len(trace) // 2, len(trace) - 1):
-        t, sc, w, h, mv = trace[i]
-        _, alone, st = serve(gpu, scenes, [(0.0, sc, w, h, mv)])
-        assert st["completed"] == 1
+    srv, ctxs = make_server(gpu, scenes)
+    for i, (t, sc, w, h, mv) in enumerate(trace):
+        reqs, alone = requests([(0.0, sc, w, h, mv)])
+        reqs[0].arrival = srv.now()
+        srv.run_trace(reqs)
+        assert reqs[0].status == 0
         assert np.array_equal(alone[0], mixed[i]), i
+    srv.destroy()
+    for c in ctxs:
+        c.destroy()
+
+
+@pytest.mark.slow
+def test_served_sample_of_the_benchmark_scenes(gpu, oracle):
+    """A seeded sample of requests from the serving benchmark's own trace (32 resident scenes
+    of 1k-500k triangles with 256^2-2048^2 textures, resolutions up to 1920x1080), served in
+    one burst, against the oracle rendering the same calls."""
+    import concurrent.futures as cf
+    import os
+
+    scenes = W.serve_scenes(32)
+    trace = W.serve_trace(60.0, 2000.0, seed=6)
+    pick = sorted(np.random.default_rng(62).choice(len(trace), size=12, replace=False))
+    sample = [(0.0,) + tuple(trace[int(i)][1:]) for i in pick]
+    reqs, outs, stats = serve(gpu, scenes, sample, executors=2, max_batch=64)
+    assert stats["completed"] == len(sample) and stats["failed"] == 0, stats
+
+    def check(i):
+        _, sc, w, h, mv = sample[i]
+        want = oracle_frame(oracle, scenes[sc], w, h, mv)
+        d = np.abs(want.view(np.uint8).astype(np.int16) - outs[i].view(np.uint8).astype(np.int16))
+        assert d.max() <= 1, (sc, w, h, int(d.max()))
+
+    order = sorted(range(len(sample)), key=lambda i: -W.scene_triangles(scenes[sample[i][1]]))
+    with cf.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        list(ex.map(check, order))
 
 
 def request_cost(gpu, scene, w, h):

@@ -35,6 +35,8 @@ class Scene:
         self.cmds.append((name, tuple(args)))
 
     def play(self, ctx, start=0, stop=None):
+        """Replays the calls [start, stop) on ctx, made current on this thread first."""
+        ctx.make_current()
         for name, args in self.cmds[start:stop]:
             ctx.call(name, *args)
 

@@ -22,8 +22,14 @@ Lines printed (one JSON object each, rank 0 only):
                sets of contexts taking turns) and, as `sequential_value`, one at a time.
   roofline     the tile raster/ROP kernel (K4): compulsory bytes per launch over its mean
                launch time (CUDA events inside the library), against the measured HBM copy peak.
+  roofline_stages  the same for each pipeline stage (vertex, setup, binning, tile), and K4's
+               issue-slot fraction (ncu warp instructions per launch over SMs x 4 x clock x time).
+  parity       the timed frames read back and compared with the CPU oracle rendering the same
+               inputs: colour max error and mismatching-pixel fraction, depth and stencil
+               mismatches (serving: a seeded sample of requests, colour only).
   cpu_baseline the CPU oracle (a restatement of MyTinyGL's renderer) on all host cores, one
-               context per thread, on a bounded sample of the same workload.
+               context per thread, on a bounded sample of the same workload; also on one
+               thread and built with MyTinyGL's shipped flags, with the CPU model.
 --impl reference times that CPU implementation as the measured arm.
 Several GPUs run independent replicas (one process per GPU, no collective on the data path).
 """
@@ -119,6 +125,53 @@ def measured_peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+POST_VERTEX_BYTES = 48  # post-transform vertex written by K1, read by K2
+REC_BOX_BYTES = 80      # record words binning reads: screen vertices, box, area, edge differences
+PAIR_BYTES = 8          # (tile, record) pair written by binning
+
+
+def ncu_instructions(workload):
+    """Warp instructions per K4 launch (smsp__inst_executed.sum) from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "ncu_k4_instructions.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == workload and parts[1] == "k_tile":
+            return float(parts[2])
+    return None
+
+
+def stage_rooflines(workload, vertices, vertex_bytes, rec, pairs, npix, tex, phase_ms, peak, sms, sm_mhz):
+    """Per-stage HBM fractions from each stage's compulsory bytes (inputs read once, outputs
+    written once) over its measured time, and K4's issue-slot fraction: warp instructions
+    per launch (ncu) over the issue slots of its measured time (SMs x 4 schedulers x clock).
+      K1 vertex:  attribute bytes read + vertices x 48 (post-transform vertex written)
+      K2 setup:   vertices x 48 (read once) + records x 224 (written)
+      K3 binning: records x 80 (box and edge words read) + pairs x 8 (written)
+      K4 tile:    pixels x 9 + pairs x 4 + records x 224 + texture bytes"""
+    stages = {
+        "k1_vertex": (vertex_bytes + vertices * POST_VERTEX_BYTES, phase_ms.get("vertex")),
+        "k2_setup": (vertices * POST_VERTEX_BYTES + rec * REC_BYTES, phase_ms.get("setup")),
+        "k3_bin": (rec * REC_BOX_BYTES + pairs * PAIR_BYTES, phase_ms.get("bin")),
+        "k4_tile": (npix * 9 + pairs * 4 + rec * REC_BYTES + tex, phase_ms.get("tile")),
+    }
+    out = {}
+    for k, (b, ms) in stages.items():
+        gbs = b / (ms / 1e3) / 1e9 if ms else None
+        out[k] = {"algorithmic_bytes": int(b), "ms": ms, "achieved_gbs": round(gbs, 2) if gbs else None,
+                  "frac": round(gbs / peak, 5) if gbs else None}
+    inst = ncu_instructions(workload)
+    t4 = phase_ms.get("tile")
+    if inst and t4 and sm_mhz:
+        slots = sms * 4 * sm_mhz * 1e6 * t4 / 1e3
+        out["k4_tile"]["issue"] = {"warp_instructions": int(inst), "issue_slots": int(slots),
+                                   "frac": round(inst / slots, 4),
+                                   "how": "ncu smsp__inst_executed.sum per launch (profiles/ncu_k4_instructions.txt) "
+                                          "over SMs x 4 schedulers x median SM clock x measured K4 time"}
+    return out
 
 
 def ncu_traffic(workload):
@@ -459,6 +512,10 @@ def run_ours(args, spec):
         "gpu_launches": int(st["kernel_launches"]),
         "clocks": clocks.summary(),
     }
+    out["roofline_stages"] = stage_rooflines(
+        spec["name"], st["vertices"] / args.steps, st["vertex_bytes"] / args.steps, rec, pairs, npix, tex_bytes,
+        out["phase_ms"], peak, torch.cuda.get_device_properties(local).multi_processor_count,
+        out["clocks"].get("sm_mhz"))
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(spec, args.cpu_seconds)
     if rank == 0 and gpu_out is not None:
@@ -713,6 +770,11 @@ def run_batch(args, spec):
         "gpu_launches": int(bst["kernel_launches"]),
         "clocks": clocks.summary(),
     }
+    nb = max(1, bst["batches"])
+    out["roofline_stages"] = stage_rooflines(
+        out["config"]["workload"], bst["vertices"] / nb, bst["vertex_bytes"] / nb, rec, pairs, npix, tex,
+        out["phase_ms"], peak, torch.cuda.get_device_properties(local).multi_processor_count,
+        out["clocks"].get("sm_mhz"))
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_batch_baseline(args.cpu_seconds)
     if rank == 0 and gpu_frames is not None:
@@ -984,7 +1046,8 @@ def cpu_batch_baseline(seconds):
     wall_s = cpu_batch_frames(_oracle_lib(shipped=True), sample, threads)
     return {"value": round(len(sample) / wall, 4), "unit": "frames/s", "cores": threads, "kind": "port",
             "cpu_model": cpu_model(), "build": STRICT_BUILD,
-            "sample": (f"every {k}th frame of the 256-frame batch ({len(sample)} frames, whole frames), "
+            "sample": (f"{'every frame' if k == 1 else f'every {k}th frame'} of the 256-frame batch "
+                       f"({len(sample)} frames, whole frames), "
                        f"one oracle context per frame on {threads} threads"), "wall_s": round(wall, 2),
             "one_thread": {"value": round(len(one) / wall1, 4), "unit": "frames/s", "cores": 1,
                            "sample": f"{len(one)} whole frames (every 8th of the sample) on one thread"},
@@ -1115,7 +1178,8 @@ def run_reference(args, spec):
             cpu_batch_frames(lib, sample, threads)
         walls = [cpu_batch_frames(lib, sample, threads) for _ in range(args.steps)]
         fps = len(sample) / statistics.median(walls)
-        desc = (f"every {k}th frame of the 256-frame batch ({len(sample)} whole frames) per step, one oracle "
+        desc = (f"{'every frame' if k == 1 else f'every {k}th frame'} of the 256-frame batch ({len(sample)} whole "
+                f"frames) per step, one oracle "
                 f"context per frame on {threads} threads")
         return line(fps, statistics.median(walls) * 1e3, batch_config(spec, W.uneven_batch(BATCH_FRAMES, use_vbo=False), world),
                     "synthetic (seeded; mytinygl_gb300/workloads.py uneven_batch)", desc)

@@ -150,6 +150,8 @@ typedef struct {
     uint64_t staged_bytes;         /* client data (attributes, indices, state ids) staged */
     uint64_t allocations;          /* device or page-locked allocations made for this context's
                                       passes (scratch, staging areas) */
+    uint64_t vertices;             /* vertex slots transformed by the vertex stage */
+    uint64_t vertex_bytes;         /* attribute bytes those slots read (enabled arrays) */
 } mtgl_stats;
 
 /* Device time per pipeline phase, summed over the passes since profiling was enabled
@@ -242,6 +244,7 @@ typedef struct {
     uint64_t graph_captures, graph_replays, overflow_reruns, kernel_launches;
     uint32_t record_capacity, pair_capacity;
     int32_t tile_size, ctas;
+    uint64_t vertices, vertex_bytes; /* as in mtgl_stats, over the batch's passes */
 } mtgl_batch_stats;
 
 /* The defaults mtgl_dev_batch_create uses for zero fields. */

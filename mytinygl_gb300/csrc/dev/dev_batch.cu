@@ -394,6 +394,8 @@ int mtgl_dev_batch_add(mtgl_batch *b, mtgl_dev *src, mtgl_dev *target)
     b->open_tris += b->passes.back().tris;
     src->stats.passes++;
     src->stats.input_triangles += b->passes.back().tris;
+    src->stats.vertices += b->passes.back().slots;
+    src->stats.vertex_bytes += b->passes.back().vbytes;
     return MTGL_OK;
 }
 
@@ -446,6 +448,10 @@ int mtgl_dev_batch_launch(mtgl_batch *b)
     b->stats.batches++;
     b->stats.frames += b->frames.size();
     b->stats.input_triangles += tris;
+    for (const Pass &p : b->passes) {
+        b->stats.vertices += p.slots;
+        b->stats.vertex_bytes += p.vbytes;
+    }
     b->stats.ctas = b->run.ctas;
     return MTGL_OK;
 }

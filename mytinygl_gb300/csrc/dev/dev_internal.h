@@ -86,6 +86,7 @@ struct Pass {
     std::vector<mtgl_raster_state> raster_src;  // for de-duplication
     bool needs_eye = false;
     uint64_t slots = 0, tris = 0;
+    uint64_t vbytes = 0;  // attribute bytes the vertex stage reads for the pass's slots
 
     bool empty() const { return clears.empty() && draws.empty(); }
     void reset();

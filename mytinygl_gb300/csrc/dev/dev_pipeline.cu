@@ -183,7 +183,7 @@ void Pass::reset()
     rasters.clear();
     raster_src.clear();
     needs_eye = false;
-    slots = tris = 0;
+    slots = tris = vbytes = 0;
 }
 
 // ------------------------------------------------------------------ scratch

@@ -136,6 +136,9 @@ uint32_t push_vstates(mtgl_dev *d, const mtgl_vertex_state *vs, uint32_t n)
 }
 
 // Resolve one attribute stream. Client memory is copied for element range [lo, hi].
+// bytes of one element of an enabled array (what the vertex stage reads per slot)
+uint64_t attr_bytes(const mtgl_attrib &a) { return a.enabled ? (uint64_t)a.size * (a.type == GL_FLOAT ? 4u : 1u) : 0u; }
+
 int resolve_attr(mtgl_dev *d, const mtgl_attrib &a, int64_t lo, int64_t hi, DevAttrib &out, int64_t &off)
 {
     memset(&out, 0, sizeof(out));
@@ -208,6 +211,8 @@ int flush_pass(mtgl_dev *d)
     if ((st = d->stage.mark_uploaded(d->x.stream))) return st;
     d->stats.passes++;
     d->stats.input_triangles += P.tris;
+    d->stats.vertices += P.slots;
+    d->stats.vertex_bytes += P.vbytes;
     d->stats.setup_triangles += o.nrec;
     d->stats.bin_entries += o.npairs;
     d->stats.kernel_launches += (uint64_t)o.launches;
@@ -516,6 +521,8 @@ int mtgl_dev_draw(mtgl_dev *d, const mtgl_draw *dr)
     D.tri_base = (uint32_t)P.tris;
     D.tri_count = (uint32_t)ntri;
     P.slots += D.vslot_count;
+    P.vbytes += (uint64_t)D.vslot_count * (attr_bytes(dr->position) + attr_bytes(dr->color) +
+                                           attr_bytes(dr->texcoord) + attr_bytes(dr->normal));
     P.tris += ntri;
     P.draws.push_back(p);
     d->stats.staged_bytes += d->stage.used - staged0;
@@ -793,6 +800,8 @@ int flush_pass_noalloc(mtgl_dev *d)
     if ((st = d->stage.mark_uploaded(d->x.stream))) return st;
     d->stats.passes++;
     d->stats.input_triangles += P.tris;
+    d->stats.vertices += P.slots;
+    d->stats.vertex_bytes += P.vbytes;
     d->stats.setup_triangles += o.nrec;
     d->stats.bin_entries += o.npairs;
     d->stats.kernel_launches += (uint64_t)o.launches;

@@ -72,7 +72,7 @@ WORKLOADS["serve"] = dict(builder=None, full_tris=None, name="serve_32_scenes_po
                                 "256^2-2048^2 mipmapped textures), Poisson arrivals at 2,000 req/s, resolution "
                                 "uniform over 256^2, 512^2, 1280x720, 1920x1080, modelview from the request "
                                 "seed, 40 GiB framebuffer + pipeline-scratch budget"))
-REC_BYTES = 224  # triangle record written by the setup kernel, read by the tile kernel
+REC_BYTES = 240  # triangle record written by the setup kernel, read by the tile kernel
 BATCH_FRAMES = 256  # frames per step of the batch workload (--frames changes it for profiling)
 E2E_SETS = 3  # context sets the end-to-end batch measurement keeps in flight
 

@@ -526,6 +526,40 @@ __device__ __forceinline__ float depth_lower_bound(const DevRaster &R, float z0,
     return fminf(dlo, dhi);
 }
 
+// The depth plane of a triangle record (R_ZP0..R_ZM, read by depth_plane_bound). Only for
+// records whose edge values are exact integers over the box (depth_rejection's condition)
+// and finite vertex depths. With u = 2^-24, S0 = sum |b_i z_i| at (minX, minY), SX = sum
+// |z_i EA_i| / |area|, SY = sum |z_i EB_i| / |area|, W, H the box's extents and Z = max |z_i|,
+// the errors are at most: a covered fragment's z below Z* by 5u Z (b_i >= 0 sum to one);
+// P0 from Z*(minX, minY) by 5u S0 (the fragment formula at that point); GX, GY from the
+// exact slopes by 5u SX, 5u SY, so the plane by 5u (SX W + SY H) over the box; the
+// evaluation by 4u (S0 + SX W + SY H) and the subtraction by u of the result. M takes
+// 16u times the sum, nearly twice what these need, which also absorbs the roundings of M.
+// tests/test_arith.py checks the bound against every covered pixel of random triangles.
+__device__ __forceinline__ float4 depth_plane(float z0, float z1, float z2, float fx0, float fy0, float fx1, float fy1,
+                                              float fx2, float fy2, float area, float inv_area, int32_t minX,
+                                              int32_t minY, int32_t maxX, int32_t maxY)
+{
+    const float ea0 = fy2 - fy1, eb0 = fx2 - fx1, ea1 = fy0 - fy2, eb1 = fx0 - fx2, ea2 = fy1 - fy0, eb2 = fx1 - fx0;
+    const float px = (float)minX, py = (float)minY;
+    // the fragment formula at (minX, minY) (edge values exact integers there)
+    const float e0 = (px - fx1) * ea0 - (py - fy1) * eb0;
+    const float e1 = (px - fx2) * ea1 - (py - fy2) * eb1;
+    const float e2 = (px - fx0) * ea2 - (py - fy0) * eb2;
+    const float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
+    const float p0 = b0 * z0 + b1 * z1 + b2 * z2;
+    const float gx = (z0 * ea0 + z1 * ea1 + z2 * ea2) / area;
+    const float gy = -((z0 * eb0 + z1 * eb1 + z2 * eb2) / area);
+    const float aa = fabsf(area);
+    const float s0 = fabsf(b0 * z0) + fabsf(b1 * z1) + fabsf(b2 * z2);
+    const float sx = (fabsf(z0 * ea0) + fabsf(z1 * ea1) + fabsf(z2 * ea2)) / aa;
+    const float sy = (fabsf(z0 * eb0) + fabsf(z1 * eb1) + fabsf(z2 * eb2)) / aa;
+    const float zabs = fmaxf(fmaxf(fabsf(z0), fabsf(z1)), fabsf(z2));
+    const float m = 0x1p-20f * (s0 + sx * (float)(maxX - minX) + sy * (float)(maxY - minY) + zabs) + 1e-37f;
+    if (!isfinite(p0) || !isfinite(gx) || !isfinite(gy) || !isfinite(m)) return make_float4(0.0f, 0.0f, 0.0f, INFINITY);
+    return make_float4(p0, gx, gy, m);
+}
+
 // ------------------------------------------------------------------ points and lines
 
 // Depth writes with a function that can raise stored depths (the tile kernel's depth
@@ -874,6 +908,10 @@ __device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t r
                            (((rs.depth_func - GL_NEVER) & 7u) << kRecDepthFuncShift);
     r4[12] = make_float4(__uint_as_float(flags), fy2 - fy1, fx2 - fx1, fy0 - fy2);
     r4[13] = make_float4(fx0 - fx2, fy1 - fy0, fx1 - fx0, __uint_as_float(frame));
+    r4[14] = (zc == ZC_LESS || zc == ZC_LEQUAL) && R.default_depth_range
+                 ? depth_plane(a.clip.z, b.clip.z, c.clip.z, fx0, fy0, fx1, fy1, fx2, fy2, area, inv_area, minX, minY,
+                               maxX, maxY)
+                 : make_float4(0.0f, 0.0f, 0.0f, INFINITY);
     if (eyerec) {
         const float3 aep = cv_ep(a), aen = cv_en(a), bep = cv_ep(b), ben = cv_en(b), cep = cv_ep(c), cen = cv_en(c);
         float4 *e4 = reinterpret_cast<float4 *>(eyerec);

@@ -46,12 +46,58 @@ __device__ __forceinline__ float warp_max_depth(float dep, bool in_fb)
 
 constexpr uint32_t kNoPending = 0xFFFFFFFFu;
 
-// tri_may_cover_rect over the 8x4 block at (bx, by)
-__device__ __forceinline__ bool block_may_cover(const float4 *q, const float4 &q1, const float4 &q2, int bx, int by)
+// The 8x4 warp blocks of the tile at (tx0, ty0) that a record must be walked in: bit
+// r * (TS / 8) + c for the block at column c, row r. A block is set when the record's box
+// (mnx..mxx, mny..mxy) meets it and, for a triangle, when its coverage test can pass there.
+// The test is exact: the edge function (px - ax) * A - (py - ay) * B has integer-valued
+// operands, so when every product over the tile is below 2^24 in magnitude the per-pixel
+// float test has the sign of the exact integer; then each edge's largest value over a block
+// (at a corner: the function is affine) is an int32 stepped per block column and row, and a
+// block where it is negative for some edge holds no covered pixel (for a negative area the
+// signs flip). Otherwise every block the box meets is set. bb = record words 4-7 (x2, y2,
+// box min), bb2 = words 8-11 (box max, area, 1/area), q12 = words 48-51.
+template <int TS>
+__device__ __forceinline__ uint32_t block_mask(const float4 *q, const float4 &bb, const float4 &bb2, const float4 &q12,
+                                               uint32_t flags, int tx0, int ty0, int mnx, int mny, int mxx, int mxy)
 {
-    if (!(q2.z > 0.0f) && !(q2.z < 0.0f)) return false;
-    const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
-    return tri_may_cover_rect(q0, q1, q2, q12, q13, (float)bx, (float)(bx + 7), (float)by, (float)(by + 3));
+    constexpr int kWX = TS / 8;
+    if (mxx < tx0 || mnx > tx0 + TS - 1 || mxy < ty0 || mny > ty0 + TS - 1) return 0u;
+    const int c0 = max(mnx - tx0, 0) >> 3, c1 = min(mxx - tx0, TS - 1) >> 3;
+    const int r0 = max(mny - ty0, 0) >> 2, r1 = min(mxy - ty0, TS - 1) >> 2;
+    uint32_t box = 0u;
+    for (int r = r0; r <= r1; r++)
+        for (int c = c0; c <= c1; c++) box |= 1u << (r * kWX + c);
+    if (((flags >> kRecTypeShift) & 3u) != REC_TRI) return box;
+    const float area = bb2.z;
+    if (!(area > 0.0f) && !(area < 0.0f)) return 0u;  // zero or NaN area: the test never passes
+    const float4 q0 = __ldg(q + 0), q13 = __ldg(q + 13);
+    const float ax[3] = {q0.z, bb.x, q0.x}, ay[3] = {q0.w, bb.y, q0.y};
+    const float ea[3] = {q12.y, q12.w, q13.y}, eb[3] = {q12.z, q13.x, q13.z};
+    const bool pos = area > 0.0f;
+    int e00[3], sx[3], sy[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        constexpr float kLim = 16777216.0f;  // 2^24
+        if (!(fabsf(ax[k]) < kLim && fabsf(ay[k]) < kLim && fabsf(ea[k]) < kLim && fabsf(eb[k]) < kLim)) return box;
+        const int iax = (int)ax[k], iay = (int)ay[k];
+        const int a = pos ? (int)ea[k] : -(int)ea[k], b = pos ? (int)eb[k] : -(int)eb[k];
+        const long long mx = max(llabs((long long)tx0 - iax), llabs((long long)tx0 + TS - 1 - iax)) * llabs((long long)a);
+        const long long my = max(llabs((long long)ty0 - iay), llabs((long long)ty0 + TS - 1 - iay)) * llabs((long long)b);
+        if (mx >= (1ll << 24) || my >= (1ll << 24)) return box;
+        // largest over block (0, 0) at its right column when a >= 0, its top row when b >= 0
+        e00[k] = (tx0 + (a >= 0 ? 7 : 0) - iax) * a - (ty0 + (b >= 0 ? 0 : 3) - iay) * b;
+        sx[k] = a * 8;
+        sy[k] = b * 4;
+    }
+    uint32_t mask = 0u;
+    for (int r = r0; r <= r1; r++)
+        for (int c = c0; c <= c1; c++) {
+            bool ok = true;
+#pragma unroll
+            for (int k = 0; k < 3; k++) ok = ok && e00[k] + c * sx[k] - r * sy[k] >= 0;
+            if (ok) mask |= 1u << (r * kWX + c);
+        }
+    return mask;
 }
 
 // The colour stages of a fragment (raster.c:582-705): colour interpolation (or the flat
@@ -388,6 +434,12 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
     constexpr int kWarpsX = TS / 8;  // 8x4-pixel warp blocks per tile row band
     constexpr uint32_t kNoTile = 0xFFFFFFFFu, kSkipTile = 0xFFFFFFFEu;
     __shared__ uint32_t s_tile, s_frame;
+    // a super-chunk of the tile's list, scanned once by the CTA (one record per thread)
+    constexpr int kSuper = TS * TS < 256 ? TS * TS : 256;
+    __shared__ uint32_t s_idx[kSuper], s_flags[kSuper], s_mask[kSuper];
+    __shared__ float s_dmin[kSuper];
+    __shared__ int4 s_box[kSuper];
+    __shared__ float4 s_plane[kSuper];
 
     if (A.guard && (A.guard[0] > A.records_cap || A.guard[1] > A.pairs_cap)) return;
 
@@ -483,85 +535,110 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
         float wzmax = warp_max_depth(dep, in_fb);
         uint32_t pend = kNoPending;  // record whose deferred colour the pixel still owes
 
-        // Each warp walks the tile's list on its own: no barrier between warps, which differ
-        // in how many records meet their 8x4 block. Record words are read through L1 with
-        // all lanes on one address (a broadcast); the CTA's warps share those lines.
+        // The tile's list is walked in super-chunks of kSuper records. The CTA scans each
+        // super-chunk once: thread t loads record t's box and edge words and finds the 8x4
+        // warp blocks the triangle can cover (the exact edge test per block), so the record
+        // is read from memory once per CTA rather than once per warp. Each warp then walks the
+        // super-chunk's records that meet its block, 32 at a time, from shared memory.
         const float4 *recs4 = reinterpret_cast<const float4 *>(A.records);
-        for (uint32_t base = 0; base < count; base += kChunk) {
-            const int n = (int)min((uint32_t)kChunk, count - base);
-            // Lane j tests record base+j against the warp: its bbox must meet the warp's block,
-            // and the depth rejection is tried with the warp's max depth as of now. That value
-            // is still an upper bound when record j is reached unless an earlier record of the
-            // step may raise depths, so rejection is only taken when none before j can. The set
-            // bits, lowest first, are this warp's records of the step in submission order.
-            uint32_t idx = 0, flags = 0;
-            float dmin = 0.0f;
-            bool take = false;
-            if (lane < n) {
-                idx = __ldg(A.tile_vals + start + base + lane);
+        for (uint32_t sbase = 0; sbase < count; sbase += kSuper) {
+            const int sn = (int)min((uint32_t)kSuper, count - sbase);
+            __syncthreads();  // the previous super-chunk's buffers are free
+            if ((int)threadIdx.x < sn) {
+                const uint32_t idx = __ldg(A.tile_vals + start + sbase + threadIdx.x);
                 const float4 *q = recs4 + (size_t)idx * (kRecWords / 4);
-                const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2);
-                take = !(__float_as_int(bb2.x) < wx0 || __float_as_int(bb.z) > wx0 + 7 ||
-                         __float_as_int(bb2.y) < wy0 || __float_as_int(bb.w) > wy0 + 3);
-                flags = __float_as_uint(__ldg(reinterpret_cast<const float *>(q) + R_FLAGS));
-                dmin = __ldg(reinterpret_cast<const float *>(q) + R_DMIN);
-                // a triangle that meets the block's box but none of its pixels is not taken
-                if (take && ((flags >> kRecTypeShift) & 3u) == REC_TRI) take = block_may_cover(q, bb, bb2, wx0, wy0);
+                const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2), q12 = __ldg(q + 12);
+                const uint32_t flags = __float_as_uint(q12.x);
+                const int mnx = __float_as_int(bb.z), mny = __float_as_int(bb.w);
+                const int mxx = __float_as_int(bb2.x), mxy = __float_as_int(bb2.y);
+                const uint32_t zc = (flags >> 1) & 3u;
+                s_idx[threadIdx.x] = idx;
+                s_flags[threadIdx.x] = flags;
+                s_dmin[threadIdx.x] = __ldg(reinterpret_cast<const float *>(q) + R_DMIN);
+                s_box[threadIdx.x] = make_int4(mnx, mny, mxx, mxy);
+                if (zc == ZC_LESS || zc == ZC_LEQUAL) s_plane[threadIdx.x] = __ldg(q + 14);
+                s_mask[threadIdx.x] = block_mask<TS>(q, bb, bb2, q12, flags, tx * TS, ty * TS, mnx, mny, mxx, mxy);
             }
-            const uint32_t raise_mask = __ballot_sync(0xffffffffu, (flags & kFlagRaisesDepth) != 0);
-            const uint32_t zc_l = (flags >> 1) & 3u;
-            if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
-                if (zc_l == ZC_NEVER || (zc_l != ZC_NONE && (dmin > wzmax || (zc_l == ZC_LESS && dmin == wzmax))))
-                    take = false;
-            }
-            uint32_t todo = __ballot_sync(0xffffffffu, take);
-            if (ROUNDS) {
-                uint32_t cov = 0;
-                while (todo) {
-                    const int j = __ffs(todo) - 1;
-                    todo &= todo - 1;
-                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
-                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                    const float4 *q = recs4 + (size_t)ridx * (kRecWords / 4);
-                    const float4 q1 = __ldg(q + 1), q2 = __ldg(q + 2);
-                    bool in = !(px < __float_as_int(q1.z) || px > __float_as_int(q2.x) ||
-                                py < __float_as_int(q1.w) || py > __float_as_int(q2.y));
-                    if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {  // points and lines test when shaded
-                        const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
-                        const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
-                        const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
-                        const float e2 = (fpx - q0.x) * q13.y - (fpy - q0.y) * q13.z;
-                        const float area = q2.z;
-                        in = in && ((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) ||
-                                    (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0));
+            __syncthreads();
+            for (int g = 0; g < sn; g += kChunk) {
+                const int n = min(kChunk, sn - g);
+                // Lane j takes record g+j when it meets the warp's block; the depth rejection is
+                // tried with the warp's max depth as of now and the record's depth bound over the
+                // block. That value is still an upper bound when record j is reached unless an
+                // earlier record of the step may raise depths, so rejection is only taken when
+                // none before j can. The set bits, lowest first, are this warp's records of the
+                // step in submission order.
+                uint32_t idx = 0, flags = 0;
+                float dmin = 0.0f;
+                bool take = false;
+                if (lane < n) {
+                    const int sl = g + lane;
+                    take = ((s_mask[sl] >> warp) & 1u) != 0;
+                    idx = s_idx[sl];
+                    flags = s_flags[sl];
+                    dmin = s_dmin[sl];
+                    const uint32_t zcl = (flags >> 1) & 3u;
+                    if (take && (zcl == ZC_LESS || zcl == ZC_LEQUAL)) {
+                        const int4 b = s_box[sl];
+                        dmin = fmaxf(dmin, depth_plane_bound(s_plane[sl], b.x, b.y, max(wx0, b.x), min(wx0 + 7, b.z),
+                                                             max(wy0, b.y), min(wy0 + 3, b.w)));
                     }
-                    if (in) cov |= 1u << j;
                 }
-                while (__any_sync(0xffffffffu, cov != 0)) {
-                    const int j = cov ? __ffs(cov) - 1 : 0;
-                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
-                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                    bool wrote = false;
-                    if (cov) {
-                        cov &= cov - 1;
-                        wrote = shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
+                const uint32_t raise_mask = __ballot_sync(0xffffffffu, (flags & kFlagRaisesDepth) != 0);
+                const uint32_t zc_l = (flags >> 1) & 3u;
+                if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
+                    if (zc_l == ZC_NEVER || (zc_l != ZC_NONE && (dmin > wzmax || (zc_l == ZC_LESS && dmin == wzmax))))
+                        take = false;
+                }
+                uint32_t todo = __ballot_sync(0xffffffffu, take);
+                if (ROUNDS) {
+                    uint32_t cov = 0;
+                    while (todo) {
+                        const int j = __ffs(todo) - 1;
+                        todo &= todo - 1;
+                        const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                        const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                        const float4 *q = recs4 + (size_t)ridx * (kRecWords / 4);
+                        const float4 q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+                        bool in = !(px < __float_as_int(q1.z) || px > __float_as_int(q2.x) ||
+                                    py < __float_as_int(q1.w) || py > __float_as_int(q2.y));
+                        if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {  // points and lines test when shaded
+                            const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
+                            const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
+                            const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
+                            const float e2 = (fpx - q0.x) * q13.y - (fpy - q0.y) * q13.z;
+                            const float area = q2.z;
+                            in = in && ((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) ||
+                                        (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0));
+                        }
+                        if (in) cov |= 1u << j;
                     }
-                    if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
-                }
-            } else {
-                while (todo) {
-                    const int j = __ffs(todo) - 1;
-                    todo &= todo - 1;
-                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
-                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                    const float rdmin = __shfl_sync(0xffffffffu, dmin, j);
-                    // warp-uniform rejection: no fragment of this triangle can pass the depth test here
-                    const uint32_t zc = (rflags >> 1) & 3u;
-                    if (zc == ZC_NEVER || (zc != ZC_NONE && (rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax))))
-                        continue;
-                    const bool wrote =
-                        shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
-                    if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
+                    while (__any_sync(0xffffffffu, cov != 0)) {
+                        const int j = cov ? __ffs(cov) - 1 : 0;
+                        const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                        const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                        bool wrote = false;
+                        if (cov) {
+                            cov &= cov - 1;
+                            wrote = shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
+                        }
+                        if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
+                    }
+                } else {
+                    while (todo) {
+                        const int j = __ffs(todo) - 1;
+                        todo &= todo - 1;
+                        const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                        const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                        const float rdmin = __shfl_sync(0xffffffffu, dmin, j);
+                        // warp-uniform rejection: no fragment of this triangle can pass the depth test here
+                        const uint32_t zc = (rflags >> 1) & 3u;
+                        if (zc == ZC_NEVER || (zc != ZC_NONE && (rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax))))
+                            continue;
+                        const bool wrote =
+                            shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
+                        if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
+                    }
                 }
             }
         }

@@ -20,7 +20,7 @@ namespace mtgl {
 constexpr int kTileShiftMin = 3;     // tile edges of 8, 16 or 32 pixels (one CTA per tile)
 constexpr int kTileShiftMax = 5;
 constexpr int kTileShiftPlain = 4;   // 16x16 tiles for single-frame passes
-constexpr int kRecWords = 56;        // words per triangle record (224 bytes)
+constexpr int kRecWords = 60;        // words per triangle record (240 bytes)
 constexpr int kEyeWords = 20;        // words per triangle eye-space record (per-fragment lighting)
 
 // Triangle record written by the setup kernel, read by the tile kernel (raster.c:451-529
@@ -40,7 +40,10 @@ enum RecField {
     R_RASTER = 47,                            // uint32 raster-state index
     R_FLAGS = 48,                             // bit 0 back facing; bits 1-2 depth rejection mode
     R_EA0 = 49, R_EB0, R_EA1, R_EB1, R_EA2, R_EB2,  // per-edge (by-ay), (bx-ax) of edge_function
-    R_FRAME = 55                              // uint32 frame index within the pass's frame table
+    R_FRAME = 55,                             // uint32 frame index within the pass's frame table
+    // the depth plane over the box, for a per-block depth bound (depth_plane_bound):
+    // z at (MINX, MINY), dz/dx, dz/dy, and the margin that makes the bound safe (+inf: none)
+    R_ZP0 = 56, R_ZGX, R_ZGY, R_ZM
 };
 
 // Depth rejection modes (R_FLAGS bits 1-2). A warp skips a triangle when no fragment of it
@@ -66,32 +69,22 @@ constexpr int kRecTypeShift = 4;
 constexpr int kRecCtlShift = 8, kRecDepthFuncShift = 20;
 __device__ __forceinline__ uint32_t rec_type(const float *r) { return (__float_as_uint(r[R_FLAGS]) >> kRecTypeShift) & 3u; }
 
-// Whether a triangle record's coverage test (the three edge functions at integer pixel
-// positions, raster.c:299-302, 534-536) can pass at some pixel of the rectangle [xl, xh] x
-// [yl, yh] (integer-valued floats). q0, q1, q2, q12, q13 are the record's 16-byte words 0, 1,
-// 2, 12 and 13. Each edge function is affine in the pixel position, so over the rectangle it
-// is largest (smallest, for a negative area) at a corner. The record's positions and per-edge
-// differences are integer-valued floats: when every product the per-pixel test forms over
-// the rectangle is below 2^24 in magnitude, those products are exact and each edge function's
-// sign is the exact one, per pixel and here alike. The rectangle is ruled out only then, and
-// only when no pixel of it can pass; otherwise it is kept. Binning (per tile) and the tile
-// kernel (per warp block) use this one test.
-__device__ __forceinline__ bool tri_may_cover_rect(const float4 &q0, const float4 &q1, const float4 &q2,
-                                                   const float4 &q12, const float4 &q13, float xl, float xh, float yl,
-                                                   float yh)
+// Lower bound of the depth of every fragment a triangle record can write in the rectangle
+// [xl, xh] x [yl, yh] of its box (inclusive pixel positions, inside the record's box).
+// The record stores a float plane p(x, y) = P0 + GX (x - MINX) + GY (y - MINY) close to the
+// exact interpolation Z*(x, y) = sum z_i e_i(x, y) / area, and a margin M covering, for every
+// covered pixel of the box, the roundings of the fragment's own z (b_i = e_i * inv_area,
+// then the sum), of P0, GX and GY, and of this evaluation (setup_fan_tri derives it). The
+// plane's minimum over the rectangle is at the corner the signs of GX and GY pick; the
+// depth mapping of the default range, (z + 1) * 0.5, is monotone. With M = +inf (no plane)
+// the result is -inf.
+__device__ __forceinline__ float depth_plane_bound(const float4 &zp, int minx, int miny, int xl, int xh, int yl,
+                                                  int yh)
 {
-    const float area = q2.z;
-    if (!(area > 0.0f) && !(area < 0.0f)) return false;  // zero or NaN area: the test never passes
-    const bool pos = area > 0.0f;
-    constexpr float kExact = 16777216.0f;  // 2^24
-    // edge function (px - ax) * A - (py - ay) * B
-    auto excludes = [&](float ax, float ay, float A, float B) -> bool {
-        const float pl = (xl - ax) * A, ph = (xh - ax) * A, ql = (yl - ay) * B, qh = (yh - ay) * B;
-        if (!(fabsf(pl) < kExact && fabsf(ph) < kExact && fabsf(ql) < kExact && fabsf(qh) < kExact)) return false;
-        return pos ? fmaxf(pl, ph) - fminf(ql, qh) < 0.0f : fminf(pl, ph) - fmaxf(ql, qh) > 0.0f;
-    };
-    return !(excludes(q0.z, q0.w, q12.y, q12.z) || excludes(q1.x, q1.y, q12.w, q13.x) ||
-             excludes(q0.x, q0.y, q13.y, q13.z));
+    const float dx = (float)((zp.y >= 0.0f ? xl : xh) - minx);
+    const float dy = (float)((zp.z >= 0.0f ? yl : yh) - miny);
+    const float z = (zp.x + zp.y * dx) + zp.z * dy - zp.w;
+    return (z + 1.0f) * 0.5f;
 }
 
 // Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).

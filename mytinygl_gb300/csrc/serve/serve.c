@@ -29,7 +29,7 @@ extern int dev_current_device(void);
 extern mtgl_dev *fe_context_device(GLState *ctx);
 
 #define POST_VERTEX_BYTES 48u
-#define RECORD_BYTES 228u  /* triangle record + its per-record tile count */
+#define RECORD_BYTES 244u  /* triangle record + its per-record tile count */
 #define PAIR_BYTES 16u     /* key, value and their sort copies */
 
 typedef struct {

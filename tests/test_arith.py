@@ -161,22 +161,37 @@ def _pixel_covered(edges, area, px, py):
     return (area > 0 and all(v >= 0 for v in e)) or (area < 0 and all(v <= 0 for v in e))
 
 
-def _rect_excluded_float(edges, area, xl, xh, yl, yh):
-    """tri_may_cover_rect negated (mtgl_device.cuh), in float32."""
-    f = np.float32
+def _block_mask_int(edges, area, tx0, ty0, box, ts=16):
+    """block_mask (k_tile.cuh) for the tile at (tx0, ty0): (blocks the box meets, blocks the
+    triangle is walked in), bit r * (ts / 8) + c for the 8x4 block at column c, row r."""
+    mnx, mny, mxx, mxy = box
+    kwx = ts // 8
+    if mxx < tx0 or mnx > tx0 + ts - 1 or mxy < ty0 or mny > ty0 + ts - 1:
+        return 0, 0
+    c0, c1 = max(mnx - tx0, 0) >> 3, min(mxx - tx0, ts - 1) >> 3
+    r0, r1 = max(mny - ty0, 0) >> 2, min(mxy - ty0, ts - 1) >> 2
+    blocks = [(r, c) for r in range(r0, r1 + 1) for c in range(c0, c1 + 1)]
+    boxbits = sum(1 << (r * kwx + c) for r, c in blocks)
     if not (area > 0 or area < 0):
-        return True
-    lim = f(16777216.0)
+        return boxbits, 0
+    pos = area > 0
+    steps = []
     for ax, ay, A, B in edges:
-        pl, ph = (f(xl) - ax) * A, (f(xh) - ax) * A
-        ql, qh = (f(yl) - ay) * B, (f(yh) - ay) * B
-        if not all(abs(v) < lim for v in (pl, ph, ql, qh)):
-            continue
-        if area > 0 and max(pl, ph) - min(ql, qh) < 0:
-            return True
-        if area < 0 and min(pl, ph) - max(ql, qh) > 0:
-            return True
-    return False
+        if not all(abs(v) < 2 ** 24 for v in (ax, ay, A, B)):
+            return boxbits, boxbits
+        ax, ay, A, B = int(ax), int(ay), int(A), int(B)
+        a, b = (A, B) if pos else (-A, -B)
+        if max(abs(tx0 - ax), abs(tx0 + ts - 1 - ax)) * abs(a) >= 1 << 24 or \
+                max(abs(ty0 - ay), abs(ty0 + ts - 1 - ay)) * abs(b) >= 1 << 24:
+            return boxbits, boxbits
+        e00 = (tx0 + (7 if a >= 0 else 0) - ax) * a - (ty0 + (0 if b >= 0 else 3) - ay) * b
+        assert -(1 << 31) <= e00 < (1 << 31)
+        steps.append((e00, 8 * a, 4 * b))
+    mask = 0
+    for r, c in blocks:
+        if all(e00 + c * sx - r * sy >= 0 for e00, sx, sy in steps):
+            mask |= 1 << (r * kwx + c)
+    return boxbits, mask
 
 
 def _tile_excluded_int(edges, area, tx0, ty0, tx1, ty1, ts):
@@ -209,7 +224,7 @@ def test_coverage_tests_never_drop_a_covered_pixel():
     """Random integer triangles (small, large, slivers, both orientations, some far off the
     pixels so that the exactness check is what decides): every 8x4 block the tile kernel
     skips and every tile binning drops holds no pixel the per-pixel float32 test covers, and
-    binning's int32 stepped values agree with the float corner test wherever both apply."""
+    a tile binning drops has no block the tile kernel walks."""
     rng = np.random.default_rng(7)
     ts = 16
     checked = dropped_blocks = dropped_tiles = 0
@@ -242,11 +257,18 @@ def test_coverage_tests_never_drop_a_covered_pixel():
             return x0_ <= x1_ and y0_ <= y1_ and bool(cov[y0_ - miny:y1_ - miny + 1, x0_ - minx:x1_ - minx + 1].any())
 
         assert _pixel_covered(edges, area, int(gx.flat[0]), int(gy.flat[0])) == bool(cov.flat[0])
-        for by in range(miny - miny % 4, maxy + 1, 4):
-            for bx in range(minx - minx % 8, maxx + 1, 8):
-                if _rect_excluded_float(edges, area, bx, bx + 7, by, by + 3):
-                    dropped_blocks += 1
-                    assert not any_covered(bx, bx + 7, by, by + 3), (k, bx, by)
+        box = (minx, miny, maxx, maxy)
+        masks = {}
+        for ty in range(miny // ts, maxy // ts + 1):
+            for tx in range(minx // ts, maxx // ts + 1):
+                boxbits, mask = _block_mask_int(edges, area, tx * ts, ty * ts, box, ts)
+                masks[(tx, ty)] = mask
+                assert mask & ~boxbits == 0
+                for bit in range(ts * ts // 32):
+                    if boxbits >> bit & 1 and not mask >> bit & 1:
+                        dropped_blocks += 1
+                        bx, by = tx * ts + 8 * (bit % (ts // 8)), ty * ts + 4 * (bit // (ts // 8))
+                        assert not any_covered(bx, bx + 7, by, by + 3), (k, bx, by)
         tx0, ty0, tx1, ty1 = minx // ts, miny // ts, maxx // ts, maxy // ts
         ex = _tile_excluded_int(edges, area, tx0, ty0, tx1, ty1, ts)
         if ex is None:
@@ -254,9 +276,106 @@ def test_coverage_tests_never_drop_a_covered_pixel():
         for tx, ty in ex:
             dropped_tiles += 1
             assert not any_covered(tx * ts, tx * ts + ts - 1, ty * ts, ty * ts + ts - 1), (k, tx, ty)
-        for ty in range(ty0, ty1 + 1):
-            for tx in range(tx0, tx1 + 1):
-                fl = _rect_excluded_float(edges, area, tx * ts, tx * ts + ts - 1, ty * ts, ty * ts + ts - 1)
-                assert fl == ((tx, ty) in ex), (k, tx, ty)
-                checked += 1
-    assert dropped_blocks > 2000 and dropped_tiles > 400 and checked > 4000
+            assert masks[(tx, ty)] == 0, (k, tx, ty)
+            checked += 1
+    assert dropped_blocks > 2000 and dropped_tiles > 400 and checked > 400
+
+
+# ---- the per-block depth bound (setup_fan_tri's depth plane, the tile kernel's bound)
+
+def _depth_plane_f32(z, xs, ys, area, inv_area, minx, miny, maxx, maxy):
+    """depth_plane (k_geom.cu), float32 operations in the same order."""
+    f = np.float32
+    z0, z1, z2 = (f(v) for v in z)
+    fx0, fy0, fx1, fy1, fx2, fy2 = (f(v) for v in (xs[0], ys[0], xs[1], ys[1], xs[2], ys[2]))
+    ea0, eb0, ea1, eb1, ea2, eb2 = fy2 - fy1, fx2 - fx1, fy0 - fy2, fx0 - fx2, fy1 - fy0, fx1 - fx0
+    px, py = f(minx), f(miny)
+    e0 = (px - fx1) * ea0 - (py - fy1) * eb0
+    e1 = (px - fx2) * ea1 - (py - fy2) * eb1
+    e2 = (px - fx0) * ea2 - (py - fy0) * eb2
+    b0, b1, b2 = e0 * inv_area, e1 * inv_area, e2 * inv_area
+    p0 = b0 * z0 + b1 * z1 + b2 * z2
+    gx = (z0 * ea0 + z1 * ea1 + z2 * ea2) / area
+    gy = -((z0 * eb0 + z1 * eb1 + z2 * eb2) / area)
+    aa = abs(area)
+    s0 = abs(b0 * z0) + abs(b1 * z1) + abs(b2 * z2)
+    sx = (abs(z0 * ea0) + abs(z1 * ea1) + abs(z2 * ea2)) / aa
+    sy = (abs(z0 * eb0) + abs(z1 * eb1) + abs(z2 * eb2)) / aa
+    zabs = max(abs(z0), abs(z1), abs(z2))
+    m = f(2.0 ** -20) * (s0 + sx * f(maxx - minx) + sy * f(maxy - miny) + zabs) + f(1e-37)
+    if not all(np.isfinite(v) for v in (p0, gx, gy, m)):
+        return f(0), f(0), f(0), f(np.inf)
+    return p0, gx, gy, m
+
+
+def _depth_plane_bound_f32(zp, minx, miny, xl, xh, yl, yh):
+    """depth_plane_bound (mtgl_device.cuh) in float32."""
+    f = np.float32
+    p0, gx, gy, m = zp
+    dx = f((xl if gx >= 0 else xh) - minx)
+    dy = f((yl if gy >= 0 else yh) - miny)
+    zz = (p0 + gx * dx) + gy * dy - m
+    return (zz + f(1)) * f(0.5)
+
+
+def test_depth_plane_bound_is_below_every_covered_fragment():
+    """Random integer triangles (small to a few hundred pixels, slivers, both orientations)
+    with vertex depths spread, nearly equal, or large: for every 8x4 block meeting the box,
+    the bound over the block's part of the box is at most the depth the tile kernel computes
+    for each covered pixel there (edge functions, b_i = e_i * inv_area, z = sum b_i z_i,
+    (z + 1) * 0.5, all float32), and it is not vacuous on ordinary triangles."""
+    f = np.float32
+    rng = np.random.default_rng(11)
+    blocks = tight = 0
+    for k in range(900):
+        scale = [5, 30, 120, 400][k % 4]
+        cx, cy = int(rng.integers(0, 300)), int(rng.integers(0, 300))
+        xs = [cx + int(v) for v in rng.integers(-scale, scale + 1, 3)]
+        ys = [cy + int(v) for v in rng.integers(-scale, scale + 1, 3)]
+        if k % 9 == 0:
+            xs[2] = xs[0] + (xs[1] - xs[0]) // 2 + 1  # near-degenerate sliver
+        kind = k % 5
+        if kind == 0:
+            z = rng.uniform(-1, 1, 3)
+        elif kind == 1:
+            z = 0.3 + rng.uniform(-1e-6, 1e-6, 3)
+        elif kind == 2:
+            z = rng.uniform(-1, 1, 3) * 1e4
+        elif kind == 3:
+            z = np.full(3, rng.uniform(-1, 1)) + np.array([0.0, 1e-7, -1e-7])
+        else:
+            z = rng.uniform(0.9, 1.0, 3)
+        z = [f(v) for v in z]
+        X0, Y0, X1, Y1, X2, Y2 = (f(v) for v in (xs[0], ys[0], xs[1], ys[1], xs[2], ys[2]))
+        area = (X2 - X0) * (Y1 - Y0) - (Y2 - Y0) * (X1 - X0)
+        if abs(area) < 0.5:
+            continue
+        sx_, sy_ = max(xs) - min(xs), max(ys) - min(ys)
+        if sx_ and sy_ and sx_ * sy_ >= 1 << 23:
+            continue  # depth_rejection's exactness condition: no plane
+        inv_area = f(1) / area
+        minx, maxx = max(min(xs), 0), min(max(xs), 511)
+        miny, maxy = max(min(ys), 0), min(max(ys), 511)
+        if minx > maxx or miny > maxy:
+            continue
+        zp = _depth_plane_f32(z, xs, ys, area, inv_area, minx, miny, maxx, maxy)
+        edges = _edges(xs[0], ys[0], xs[1], ys[1], xs[2], ys[2])
+        gx, gy = np.meshgrid(np.arange(minx, maxx + 1, dtype=np.float32), np.arange(miny, maxy + 1, dtype=np.float32))
+        e = [(gx - ax) * A - (gy - ay) * B for ax, ay, A, B in edges]
+        cov = (e[0] >= 0) & (e[1] >= 0) & (e[2] >= 0) if area > 0 else (e[0] <= 0) & (e[1] <= 0) & (e[2] <= 0)
+        b = [ei * inv_area for ei in e]
+        zz = b[0] * z[0] + b[1] * z[1] + b[2] * z[2]
+        depth = (zz + f(1)) * f(0.5)
+        for by in range(miny - miny % 4, maxy + 1, 4):
+            for bx in range(minx - minx % 8, maxx + 1, 8):
+                xl, xh, yl, yh = max(bx, minx), min(bx + 7, maxx), max(by, miny), min(by + 3, maxy)
+                sub = cov[yl - miny:yh - miny + 1, xl - minx:xh - minx + 1]
+                if not sub.any():
+                    continue
+                lo = _depth_plane_bound_f32(zp, minx, miny, xl, xh, yl, yh)
+                dmin = depth[yl - miny:yh - miny + 1, xl - minx:xh - minx + 1][sub].min()
+                assert lo <= dmin, (k, bx, by, float(lo), float(dmin))
+                blocks += 1
+                if kind == 0 and dmin - lo < 1e-4:
+                    tight += 1
+    assert blocks > 20000 and tight > 1000

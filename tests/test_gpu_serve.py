@@ -143,7 +143,7 @@ def request_cost(gpu, scene, w, h):
     """The server's admission cost of a request (framebuffer + pipeline-scratch estimate)."""
     cfg = G.BatchConfig()
     gpu.lib.mtgl_dev_batch_defaults(cfg)
-    per_tri = 3 * 48 + 8 + cfg.record_factor * (228 + cfg.pair_factor * 16)
+    per_tri = 3 * 48 + 8 + cfg.record_factor * (244 + cfg.pair_factor * 16)
     return w * h * 9 + int(per_tri * W.scene_triangles(scene))
 
 

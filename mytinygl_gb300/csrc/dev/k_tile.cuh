@@ -448,10 +448,12 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
     const bool have_eye = EYE && A.eye_records != nullptr;
     uint32_t frags = 0;
 
+    uint32_t next_it = 0;  // thread 0: the work item claimed for the CTA's next tile
     for (bool first = true;; first = false) {
         if (!A.ctas && !first) break;  // one tile per CTA
         // Thread 0 takes the next work item and resolves its tile and frame; two barriers per
-        // tile (the previous tile is done; the new one is published).
+        // tile (the previous tile is done; the new one is published). Persistent CTAs claim
+        // each item one tile ahead, so the queue's atomic is not waited for between tiles.
         __syncthreads();
         if (threadIdx.x == 0) {
             uint32_t it, hi;
@@ -459,7 +461,10 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                 // this launch's items: the small-record part of the list, or the rest
                 const uint32_t split = A.split ? min(*A.split, A.ntiles) : (ROUNDS ? A.ntiles : 0u);
                 hi = ROUNDS ? split : A.ntiles;
-                it = (ROUNDS ? 0u : split) + atomicAdd(A.queue + (ROUNDS ? 0 : 1), 1u);
+                const uint32_t lo = ROUNDS ? 0u : split;
+                uint32_t *head = A.queue + (ROUNDS ? 0 : 1);
+                it = first ? lo + atomicAdd(head, 1u) : next_it;
+                if (it < hi) next_it = lo + atomicAdd(head, 1u);
             } else {
                 it = blockIdx.x;
                 hi = A.ntiles;

@@ -114,6 +114,8 @@ struct TileArgs {
     const float *records;
     const float *eye_records;
     const uint32_t *tile_vals;   // record indices sorted by tile, submission order within a tile
+    uint32_t *pair_mask;         // per entry of tile_vals: the warp blocks that walk it (written
+                                 // by the tile's CTA; binning's sorted keys, no longer read)
     const uint32_t *tile_start;  // per tile
     const uint32_t *tile_count;
     const DevRaster *rasters;

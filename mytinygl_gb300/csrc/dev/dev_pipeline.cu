@@ -600,6 +600,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ta.records = records;
     ta.eye_records = eye_records;
     ta.tile_vals = rec_cap ? ba.vals : nullptr;
+    ta.pair_mask = rec_cap ? ba.keys : nullptr;
     ta.tile_start = tile_start;
     ta.tile_count = tile_count;
     ta.rasters = ga.rasters;

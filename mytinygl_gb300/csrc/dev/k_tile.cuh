@@ -434,12 +434,6 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
     constexpr int kWarpsX = TS / 8;  // 8x4-pixel warp blocks per tile row band
     constexpr uint32_t kNoTile = 0xFFFFFFFFu, kSkipTile = 0xFFFFFFFEu;
     __shared__ uint32_t s_tile, s_frame;
-    // a super-chunk of the tile's list, scanned once by the CTA (one record per thread)
-    constexpr int kSuper = TS * TS < 256 ? TS * TS : 256;
-    __shared__ uint32_t s_idx[kSuper], s_flags[kSuper], s_mask[kSuper];
-    __shared__ float s_dmin[kSuper];
-    __shared__ int4 s_box[kSuper];
-    __shared__ float4 s_plane[kSuper];
 
     if (A.guard && (A.guard[0] > A.records_cap || A.guard[1] > A.pairs_cap)) return;
 
@@ -540,110 +534,104 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
         float wzmax = warp_max_depth(dep, in_fb);
         uint32_t pend = kNoPending;  // record whose deferred colour the pixel still owes
 
-        // The tile's list is walked in super-chunks of kSuper records. The CTA scans each
-        // super-chunk once: thread t loads record t's box and edge words and finds the 8x4
-        // warp blocks the triangle can cover (the exact edge test per block), so the record
-        // is read from memory once per CTA rather than once per warp. Each warp then walks the
-        // super-chunk's records that meet its block, 32 at a time, from shared memory.
+        // The CTA first scans the tile's list once: thread t takes records t, t + CTA size, ...,
+        // loads each one's box and edge words and writes the 8x4 warp blocks the triangle can
+        // cover (the exact edge test per block) beside the record's entry. A record is then
+        // read from memory once per CTA rather than once per warp. After one barrier each warp
+        // walks the list on its own, 32 entries per step, taking those whose mask names its
+        // block: no barrier between warps, which differ in how much work their blocks hold.
         const float4 *recs4 = reinterpret_cast<const float4 *>(A.records);
-        for (uint32_t sbase = 0; sbase < count; sbase += kSuper) {
-            const int sn = (int)min((uint32_t)kSuper, count - sbase);
-            __syncthreads();  // the previous super-chunk's buffers are free
-            if ((int)threadIdx.x < sn) {
-                const uint32_t idx = __ldg(A.tile_vals + start + sbase + threadIdx.x);
-                const float4 *q = recs4 + (size_t)idx * (kRecWords / 4);
-                const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2), q12 = __ldg(q + 12);
-                const uint32_t flags = __float_as_uint(q12.x);
-                const int mnx = __float_as_int(bb.z), mny = __float_as_int(bb.w);
-                const int mxx = __float_as_int(bb2.x), mxy = __float_as_int(bb2.y);
-                const uint32_t zc = (flags >> 1) & 3u;
-                s_idx[threadIdx.x] = idx;
-                s_flags[threadIdx.x] = flags;
-                s_dmin[threadIdx.x] = __ldg(reinterpret_cast<const float *>(q) + R_DMIN);
-                s_box[threadIdx.x] = make_int4(mnx, mny, mxx, mxy);
-                if (zc == ZC_LESS || zc == ZC_LEQUAL) s_plane[threadIdx.x] = __ldg(q + 14);
-                s_mask[threadIdx.x] = block_mask<TS>(q, bb, bb2, q12, flags, tx * TS, ty * TS, mnx, mny, mxx, mxy);
+        for (uint32_t i = threadIdx.x; i < count; i += TS * TS) {
+            const uint32_t idx = __ldg(A.tile_vals + start + i);
+            const float4 *q = recs4 + (size_t)idx * (kRecWords / 4);
+            const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2), q12 = __ldg(q + 12);
+            A.pair_mask[start + i] = block_mask<TS>(q, bb, bb2, q12, __float_as_uint(q12.x), tx * TS, ty * TS,
+                                                    __float_as_int(bb.z), __float_as_int(bb.w),
+                                                    __float_as_int(bb2.x), __float_as_int(bb2.y));
+        }
+        __syncthreads();
+        for (uint32_t base = 0; base < count; base += kChunk) {
+            const int n = (int)min((uint32_t)kChunk, count - base);
+            // Lane j takes entry base+j when its mask names the warp's block; the depth
+            // rejection is tried with the warp's max depth as of now and the record's depth
+            // bound over the block. That value is still an upper bound when record j is reached
+            // unless an earlier record of the step may raise depths, so rejection is only taken
+            // when none before j can. The set bits, lowest first, are this warp's records of the
+            // step in submission order.
+            uint32_t idx = 0, flags = 0;
+            float dmin = 0.0f;
+            bool take = false;
+            if (lane < n) {
+                idx = __ldg(A.tile_vals + start + base + lane);
+                take = ((A.pair_mask[start + base + lane] >> warp) & 1u) != 0;
             }
-            __syncthreads();
-            for (int g = 0; g < sn; g += kChunk) {
-                const int n = min(kChunk, sn - g);
-                // Lane j takes record g+j when it meets the warp's block; the depth rejection is
-                // tried with the warp's max depth as of now and the record's depth bound over the
-                // block. That value is still an upper bound when record j is reached unless an
-                // earlier record of the step may raise depths, so rejection is only taken when
-                // none before j can. The set bits, lowest first, are this warp's records of the
-                // step in submission order.
-                uint32_t idx = 0, flags = 0;
-                float dmin = 0.0f;
-                bool take = false;
-                if (lane < n) {
-                    const int sl = g + lane;
-                    take = ((s_mask[sl] >> warp) & 1u) != 0;
-                    idx = s_idx[sl];
-                    flags = s_flags[sl];
-                    dmin = s_dmin[sl];
-                    const uint32_t zcl = (flags >> 1) & 3u;
-                    if (take && (zcl == ZC_LESS || zcl == ZC_LEQUAL)) {
-                        const int4 b = s_box[sl];
-                        dmin = fmaxf(dmin, depth_plane_bound(s_plane[sl], b.x, b.y, max(wx0, b.x), min(wx0 + 7, b.z),
-                                                             max(wy0, b.y), min(wy0 + 3, b.w)));
-                    }
+            if (take) {
+                const float4 *q = recs4 + (size_t)idx * (kRecWords / 4);
+                flags = __float_as_uint(__ldg(reinterpret_cast<const float *>(q) + R_FLAGS));
+                dmin = __ldg(reinterpret_cast<const float *>(q) + R_DMIN);
+                const uint32_t zcl = (flags >> 1) & 3u;
+                if (zcl == ZC_LESS || zcl == ZC_LEQUAL) {
+                    const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2);
+                    const int mnx = __float_as_int(bb.z), mny = __float_as_int(bb.w);
+                    const int mxx = __float_as_int(bb2.x), mxy = __float_as_int(bb2.y);
+                    dmin = fmaxf(dmin, depth_plane_bound(__ldg(q + 14), mnx, mny, max(wx0, mnx), min(wx0 + 7, mxx),
+                                                         max(wy0, mny), min(wy0 + 3, mxy)));
                 }
-                const uint32_t raise_mask = __ballot_sync(0xffffffffu, (flags & kFlagRaisesDepth) != 0);
-                const uint32_t zc_l = (flags >> 1) & 3u;
-                if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
-                    if (zc_l == ZC_NEVER || (zc_l != ZC_NONE && (dmin > wzmax || (zc_l == ZC_LESS && dmin == wzmax))))
-                        take = false;
+            }
+            const uint32_t raise_mask = __ballot_sync(0xffffffffu, (flags & kFlagRaisesDepth) != 0);
+            const uint32_t zc_l = (flags >> 1) & 3u;
+            if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
+                if (zc_l == ZC_NEVER || (zc_l != ZC_NONE && (dmin > wzmax || (zc_l == ZC_LESS && dmin == wzmax))))
+                    take = false;
+            }
+            uint32_t todo = __ballot_sync(0xffffffffu, take);
+            if (ROUNDS) {
+                uint32_t cov = 0;
+                while (todo) {
+                    const int j = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                    const float4 *q = recs4 + (size_t)ridx * (kRecWords / 4);
+                    const float4 q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+                    bool in = !(px < __float_as_int(q1.z) || px > __float_as_int(q2.x) ||
+                                py < __float_as_int(q1.w) || py > __float_as_int(q2.y));
+                    if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {  // points and lines test when shaded
+                        const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
+                        const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
+                        const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
+                        const float e2 = (fpx - q0.x) * q13.y - (fpy - q0.y) * q13.z;
+                        const float area = q2.z;
+                        in = in && ((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) ||
+                                    (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0));
+                    }
+                    if (in) cov |= 1u << j;
                 }
-                uint32_t todo = __ballot_sync(0xffffffffu, take);
-                if (ROUNDS) {
-                    uint32_t cov = 0;
-                    while (todo) {
-                        const int j = __ffs(todo) - 1;
-                        todo &= todo - 1;
-                        const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
-                        const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                        const float4 *q = recs4 + (size_t)ridx * (kRecWords / 4);
-                        const float4 q1 = __ldg(q + 1), q2 = __ldg(q + 2);
-                        bool in = !(px < __float_as_int(q1.z) || px > __float_as_int(q2.x) ||
-                                    py < __float_as_int(q1.w) || py > __float_as_int(q2.y));
-                        if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {  // points and lines test when shaded
-                            const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
-                            const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
-                            const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
-                            const float e2 = (fpx - q0.x) * q13.y - (fpy - q0.y) * q13.z;
-                            const float area = q2.z;
-                            in = in && ((area > 0 && e0 >= 0 && e1 >= 0 && e2 >= 0) ||
-                                        (area < 0 && e0 <= 0 && e1 <= 0 && e2 <= 0));
-                        }
-                        if (in) cov |= 1u << j;
+                while (__any_sync(0xffffffffu, cov != 0)) {
+                    const int j = cov ? __ffs(cov) - 1 : 0;
+                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                    bool wrote = false;
+                    if (cov) {
+                        cov &= cov - 1;
+                        wrote = shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
                     }
-                    while (__any_sync(0xffffffffu, cov != 0)) {
-                        const int j = cov ? __ffs(cov) - 1 : 0;
-                        const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
-                        const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                        bool wrote = false;
-                        if (cov) {
-                            cov &= cov - 1;
-                            wrote = shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
-                        }
-                        if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
-                    }
-                } else {
-                    while (todo) {
-                        const int j = __ffs(todo) - 1;
-                        todo &= todo - 1;
-                        const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
-                        const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                        const float rdmin = __shfl_sync(0xffffffffu, dmin, j);
-                        // warp-uniform rejection: no fragment of this triangle can pass the depth test here
-                        const uint32_t zc = (rflags >> 1) & 3u;
-                        if (zc == ZC_NEVER || (zc != ZC_NONE && (rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax))))
-                            continue;
-                        const bool wrote =
-                            shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
-                        if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
-                    }
+                    if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
+                }
+            } else {
+                while (todo) {
+                    const int j = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
+                    const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
+                    const float rdmin = __shfl_sync(0xffffffffu, dmin, j);
+                    // warp-uniform rejection: no fragment of this triangle can pass the depth test here
+                    const uint32_t zc = (rflags >> 1) & 3u;
+                    if (zc == ZC_NEVER || (zc != ZC_NONE && (rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax))))
+                        continue;
+                    const bool wrote =
+                        shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
+                    if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
                 }
             }
         }

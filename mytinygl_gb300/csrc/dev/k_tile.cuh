@@ -18,7 +18,6 @@
 #pragma once
 
 #include <algorithm>
-#include <mutex>
 
 #include "dev_kernels.h"
 
@@ -211,8 +210,7 @@ __device__ __forceinline__ uint32_t pending_color(const TileArgs &A, uint32_t ri
 }
 
 // One fragment of rasterize_triangle_smooth's pixel loop (raster.c:534-722) for this
-// thread's pixel. hw: the record's words 0-3, 12 and 13 (16-byte words; the warp staged
-// them in shared memory), which the coverage and depth stages read. Returns true when it wrote the depth buffer. TEX / EYE compile the
+// thread's pixel. Returns true when it wrote the depth buffer. TEX / EYE compile the
 // texturing and per-fragment lighting stages in only for passes that use them.
 //
 // DEFER (deferred colour): in a pass whose every record is a filled triangle whose raster
@@ -224,21 +222,20 @@ __device__ __forceinline__ uint32_t pending_color(const TileArgs &A, uint32_t ri
 // colour comes out exactly as if every fragment had been shaded in turn.
 template <bool TEX, bool EYE, bool DEFER>
 __device__ __forceinline__ bool shade_pixel(const TileArgs &A, uint32_t ridx, const float *__restrict__ r,
-                                            const float4 *hw,
                                             const float *__restrict__ e, bool have_eye, int px, int py, float fpx,
                                             float fpy, uint32_t &col, float &dep, uint32_t &st, uint32_t &frags,
                                             uint32_t &pend)
 {
     // the record is read as 16-byte words (RecField positions noted beside each use)
     const float4 *r4 = reinterpret_cast<const float4 *>(r);
-    const float4 q1 = hw[1];  // X2 Y2 MINX MINY
-    const float4 q2 = hw[2];  // MAXX MAXY AREA INV_AREA
+    const float4 q1 = __ldg(r4 + 1);  // X2 Y2 MINX MINY
+    const float4 q2 = __ldg(r4 + 2);  // MAXX MAXY AREA INV_AREA
     if (px < __float_as_int(q1.z) || px > __float_as_int(q2.x) || py < __float_as_int(q1.w) ||
         py > __float_as_int(q2.y))
         return false;
-    const float4 q0 = hw[0];   // X0 Y0 X1 Y1
-    const float4 q12 = hw[4];  // FLAGS EA0 EB0 EA1
-    const float4 q13 = hw[5];  // EB1 EA2 EB2 FRAME
+    const float4 q0 = __ldg(r4 + 0);   // X0 Y0 X1 Y1
+    const float4 q12 = __ldg(r4 + 12);  // FLAGS EA0 EB0 EA1
+    const float4 q13 = __ldg(r4 + 13);  // EB1 EA2 EB2 FRAME
     // edge_function at the integer pixel position (raster.c:299-302, 534-536)
     const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
     const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
@@ -248,7 +245,7 @@ __device__ __forceinline__ bool shade_pixel(const TileArgs &A, uint32_t ridx, co
     frags++;
     const float inv_area = q2.w;
     const float b0 = e0 * inv_area, b1 = e1 * inv_area, b2 = e2 * inv_area;
-    const float4 q3 = hw[3];    // Z0 Z1 Z2 DMIN
+    const float4 q3 = __ldg(r4 + 3);    // Z0 Z1 Z2 DMIN
     // the raster state, only where a stage reads more than the record carries
     auto raster = [&]() -> const DevRaster & {
         return A.rasters[min(__float_as_uint(__ldg(r + R_RASTER)), A.nrasters - 1)];
@@ -397,15 +394,14 @@ static __device__ __noinline__ PixelOut shade_prim(const TileArgs &A, const floa
 
 // One covered fragment of record `ridx` for this thread's pixel, whatever the record draws.
 template <bool TEX, bool EYE, bool DEFER>
-__device__ __forceinline__ bool shade_any(const TileArgs &A, uint32_t ridx, const float4 *hw, uint32_t rflags,
-                                          bool have_eye, int px,
+__device__ __forceinline__ bool shade_any(const TileArgs &A, uint32_t ridx, uint32_t rflags, bool have_eye, int px,
                                           int py, float fpx, float fpy, uint32_t &col, float &dep, uint32_t &st,
                                           uint32_t &frags, uint32_t &pend)
 {
     const float *r = A.records + (size_t)ridx * kRecWords;
     if (DEFER || ((rflags >> kRecTypeShift) & 3u) == REC_TRI) {  // deferred passes hold triangles only
         const float *e = have_eye ? A.eye_records + (size_t)ridx * kEyeWords : nullptr;
-        return shade_pixel<TEX, EYE, DEFER>(A, ridx, r, hw, e, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
+        return shade_pixel<TEX, EYE, DEFER>(A, ridx, r, e, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
     }
     const PixelOut po = shade_prim(A, r, px, py, col, dep);
     col = po.col;
@@ -438,9 +434,6 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
     constexpr int kWarpsX = TS / 8;  // 8x4-pixel warp blocks per tile row band
     constexpr uint32_t kNoTile = 0xFFFFFFFFu, kSkipTile = 0xFFFFFFFEu;
     __shared__ uint32_t s_tile, s_frame;
-    // dynamic: per warp and lane of a step, the taken record's words 0-3, 12, 13 (what the
-    // coverage and depth stages read), so the walk reads them from shared memory
-    extern __shared__ float4 s_hw[];
 
     if (A.guard && (A.guard[0] > A.records_cap || A.guard[1] > A.pairs_cap)) return;
 
@@ -573,28 +566,18 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                 take = ((A.pair_mask[start + base + lane] >> warp) & 1u) != 0;
             }
             if (take) {
-                // the words the fragment's coverage and depth stages read, loaded by all taken
-                // lanes at once and kept in the warp's shared slots for the walk below
                 const float4 *q = recs4 + (size_t)idx * (kRecWords / 4);
-                const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2), q3 = __ldg(q + 3), q12 = __ldg(q + 12);
-                float4 *hw = s_hw + (warp * kChunk + lane) * 6;
-                hw[0] = __ldg(q + 0);
-                hw[1] = bb;
-                hw[2] = bb2;
-                hw[3] = q3;
-                hw[4] = q12;
-                hw[5] = __ldg(q + 13);
-                flags = __float_as_uint(q12.x);
-                dmin = q3.w;
+                flags = __float_as_uint(__ldg(reinterpret_cast<const float *>(q) + R_FLAGS));
+                dmin = __ldg(reinterpret_cast<const float *>(q) + R_DMIN);
                 const uint32_t zcl = (flags >> 1) & 3u;
                 if (zcl == ZC_LESS || zcl == ZC_LEQUAL) {
+                    const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2);
                     const int mnx = __float_as_int(bb.z), mny = __float_as_int(bb.w);
                     const int mxx = __float_as_int(bb2.x), mxy = __float_as_int(bb2.y);
                     dmin = fmaxf(dmin, depth_plane_bound(__ldg(q + 14), mnx, mny, max(wx0, mnx), min(wx0 + 7, mxx),
                                                          max(wy0, mny), min(wy0 + 3, mxy)));
                 }
             }
-            __syncwarp();
             const uint32_t raise_mask = __ballot_sync(0xffffffffu, (flags & kFlagRaisesDepth) != 0);
             const uint32_t zc_l = (flags >> 1) & 3u;
             if (take && (raise_mask & ((1u << lane) - 1u)) == 0) {
@@ -609,12 +592,12 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                     todo &= todo - 1;
                     const uint32_t ridx = __shfl_sync(0xffffffffu, idx, j);
                     const uint32_t rflags = __shfl_sync(0xffffffffu, flags, j);
-                    const float4 *hw = s_hw + (warp * kChunk + j) * 6;
-                    const float4 q1 = hw[1], q2 = hw[2];
+                    const float4 *q = recs4 + (size_t)ridx * (kRecWords / 4);
+                    const float4 q1 = __ldg(q + 1), q2 = __ldg(q + 2);
                     bool in = !(px < __float_as_int(q1.z) || px > __float_as_int(q2.x) ||
                                 py < __float_as_int(q1.w) || py > __float_as_int(q2.y));
                     if (((rflags >> kRecTypeShift) & 3u) == REC_TRI) {  // points and lines test when shaded
-                        const float4 q0 = hw[0], q12 = hw[4], q13 = hw[5];
+                        const float4 q0 = __ldg(q + 0), q12 = __ldg(q + 12), q13 = __ldg(q + 13);
                         const float e0 = (fpx - q0.z) * q12.y - (fpy - q0.w) * q12.z;
                         const float e1 = (fpx - q1.x) * q12.w - (fpy - q1.y) * q13.x;
                         const float e2 = (fpx - q0.x) * q13.y - (fpy - q0.y) * q13.z;
@@ -631,8 +614,7 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                     bool wrote = false;
                     if (cov) {
                         cov &= cov - 1;
-                        wrote = shade_any<TEX, EYE, DEFER>(A, ridx, s_hw + (warp * kChunk + j) * 6, rflags, have_eye, px, py, fpx, fpy, col,
-                                                           dep, st, frags, pend);
+                        wrote = shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
                     }
                     if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
                 }
@@ -648,8 +630,7 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                     if (zc == ZC_NEVER || (zc != ZC_NONE && (rdmin > wzmax || (zc == ZC_LESS && rdmin == wzmax))))
                         continue;
                     const bool wrote =
-                        shade_any<TEX, EYE, DEFER>(A, ridx, s_hw + (warp * kChunk + j) * 6, rflags, have_eye, px, py, fpx, fpy, col, dep,
-                                                   st, frags, pend);
+                        shade_any<TEX, EYE, DEFER>(A, ridx, rflags, have_eye, px, py, fpx, fpy, col, dep, st, frags, pend);
                     if (__any_sync(0xffffffffu, wrote)) wzmax = warp_max_depth(dep, in_fb);
                 }
             }
@@ -672,26 +653,12 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
 // k_tile.cu, so that the two halves compile in parallel.
 template <int TS, bool TEX, bool EYE, bool DEFER>
 struct TileVariant {
-    // dynamic shared memory: the staged record words of every warp's step (96 KB for 32-pixel
-    // tiles, above the default limit, so the launch raises the kernels' maximum once)
-    static constexpr size_t kSmem = (size_t)(TS * TS / 32) * kChunk * 6 * sizeof(float4);
-    static void prepare()
-    {
-        static std::once_flag once;
-        std::call_once(once, [] {
-            cudaFuncSetAttribute(k_tile<TS, TEX, EYE, false, DEFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kSmem);
-            cudaFuncSetAttribute(k_tile<TS, TEX, EYE, true, DEFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kSmem);
-        });
-    }
     static int occupancy()
     {
         static int occ = -1;
         if (occ < 0) {
-            prepare();
             int n = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tile<TS, TEX, EYE, false, DEFER>, TS * TS, kSmem) !=
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tile<TS, TEX, EYE, false, DEFER>, TS * TS, 0) !=
                 cudaSuccess)
                 n = 1;
             occ = n > 0 ? n : 1;
@@ -700,14 +667,13 @@ struct TileVariant {
     }
     static int launch(const TileArgs &a, cudaStream_t s)
     {
-        prepare();
         const unsigned grid = a.ctas ? (unsigned)std::min<uint32_t>((uint32_t)a.ctas, a.ntiles) : a.ntiles;
         if ((a.split || a.tile_area) && a.ctas && !DEFER) {  // small-record tiles by rounds, then the rest
-            k_tile<TS, TEX, EYE, true, DEFER><<<grid, TS * TS, kSmem, s>>>(a);
-            k_tile<TS, TEX, EYE, false, DEFER><<<grid, TS * TS, kSmem, s>>>(a);
+            k_tile<TS, TEX, EYE, true, DEFER><<<grid, TS * TS, 0, s>>>(a);
+            k_tile<TS, TEX, EYE, false, DEFER><<<grid, TS * TS, 0, s>>>(a);
             return 2;
         }
-        k_tile<TS, TEX, EYE, false, DEFER><<<grid, TS * TS, kSmem, s>>>(a);
+        k_tile<TS, TEX, EYE, false, DEFER><<<grid, TS * TS, 0, s>>>(a);
         return 1;
     }
 };

@@ -1,5 +1,6 @@
-"""Autotuner of the batched renderer: tile size, persistent CTAs per SM, work order and the
-record / tile-pair capacity factors, measured on the uneven-batch workload on this GPU.
+"""Autotuner of the batched renderer: tile size, persistent CTAs per SM, work order (costliest
+tiles first, or frame order) and the record / tile-pair capacity factors, measured on the
+uneven-batch workload on this GPU.
 
     python -m mytinygl_gb300.autotune [--frames 256] [--steps 5]
 
@@ -97,6 +98,7 @@ def main():
                 "#pragma once\n"
                 f"#define MTGL_TUNED_TILE_SIZE {best['tile_size']}\n"
                 f"#define MTGL_TUNED_CTAS_PER_SM {best['ctas_per_sm']}\n"
+                f"#define MTGL_TUNED_ORDER_BY_COST {best['order_by_cost']}\n"
                 f"#define MTGL_TUNED_RECORD_FACTOR {rec_factor:.2f}f\n"
                 f"#define MTGL_TUNED_PAIR_FACTOR {pair_factor:.1f}f\n")
     print(json.dumps({"best": best, "record_factor": rec_factor, "pair_factor": pair_factor}))

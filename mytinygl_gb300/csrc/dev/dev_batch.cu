@@ -227,7 +227,7 @@ void mtgl_dev_batch_defaults(mtgl_batch_config *cfg)
     cfg->record_factor = MTGL_TUNED_RECORD_FACTOR;
     cfg->pair_factor = MTGL_TUNED_PAIR_FACTOR;
     cfg->use_graph = 1;
-    cfg->order_by_cost = 1;
+    cfg->order_by_cost = MTGL_TUNED_ORDER_BY_COST;
     cfg->readback_kernel = 1;
 }
 

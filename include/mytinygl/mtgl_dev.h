@@ -176,6 +176,11 @@ int mtgl_dev_texture_create(mtgl_dev *d, mtgl_handle *out);
 /* rgba32: packed a<<24|b<<16|g<<8|r texels (graphics.h:420-434). Builds mip level 1. */
 int mtgl_dev_texture_image(mtgl_dev *d, mtgl_handle h, int32_t width, int32_t height, const uint32_t *rgba32);
 int mtgl_dev_texture_destroy(mtgl_dev *d, mtgl_handle h);
+/* Replace level `level` (>= 1) of a texture whose chain was built under
+ * MTGL_OPT_MIPMAP_CHAIN; the size must be the level's. No counterpart in the reference.
+ * Returns MTGL_ERR_INVALID when the texture has no such level or the size differs. */
+int mtgl_dev_texture_level(mtgl_dev *d, mtgl_handle h, int32_t level, int32_t width, int32_t height,
+                           const uint32_t *rgba32);
 
 /* ---- commands, executed in submission order ---- */
 /* glClear over [x0,x1) x [y0,y1) (already clamped), gl_api.c:409-457 */
@@ -209,6 +214,15 @@ void *mtgl_dev_stream(mtgl_dev *d);
  * stencil test is off. Rendering is identical either way; with it off every covered
  * fragment is counted in mtgl_stats.fragments. Applies to draws queued afterwards. */
 #define MTGL_OPT_DEPTH_REJECTION 1
+/* MTGL_OPT_MIPMAP_CHAIN (default 0): an extension with no counterpart in MyTinyGL, whose
+ * glTexImage2D accepts level 0 only and whose sampler knows level 0 and one derived level
+ * (textures.c:311-354, 457-557). With it on, a texture image given afterwards also gets
+ * every further level (each a 2x2 box filter of the one before, down to a side of 1),
+ * glTexImage2D accepts levels above 0 of matching size (replacing that level), and the
+ * mipmap filters use the whole chain: GL_*_MIPMAP_NEAREST the level nearest the triangle's
+ * LOD, GL_*_MIPMAP_LINEAR a blend of the two levels around it. Rendering is then outside
+ * parity with the reference (which clamps the LOD to level 1); with it off nothing changes. */
+#define MTGL_OPT_MIPMAP_CHAIN 2
 int mtgl_dev_set_option(mtgl_dev *d, int option, int value);
 
 /* ---- batches: many contexts' pending passes in one pipeline run ----

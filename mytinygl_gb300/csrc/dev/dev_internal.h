@@ -32,6 +32,10 @@ struct DevTextureObj {
     uint32_t *base = nullptr;
     uint32_t *mip1 = nullptr;
     int32_t w = 0, h = 0, mw = 0, mh = 0;
+    // MTGL_OPT_MIPMAP_CHAIN: levels 2.. in one allocation, and their device table
+    uint32_t *chain = nullptr;
+    DevMip *chain_tab = nullptr;
+    std::vector<DevMip> levels;  // host copy of the table (device pointers)
 };
 
 // Pending draw: a DevDraw whose pointers are patched when its pass is staged; off_* are
@@ -212,6 +216,7 @@ struct mtgl_dev {
     mtgl_stats stats{};
     uint64_t alloc_base = 0;  // allocation count at the last reset of the counters
     bool depth_rejection = true;
+    bool mipmap_chain = false;  // MTGL_OPT_MIPMAP_CHAIN
     // ordering against batches, which run on their own streams: work of this context's
     // stream that a batch must wait for, and a batch this context's stream must wait for
     cudaEvent_t tail = nullptr;

@@ -96,6 +96,8 @@ void pack_frag_state(DevRaster &R)
     f.wrap_t = rs.tex_wrap_t;
     f.min_filter = rs.tex_min_filter;
     f.mag_filter = rs.tex_mag_filter;
+    f.chain = R.chain;
+    f.chain_levels = R.chain_levels;
 }
 
 uint32_t push_raster(mtgl_dev *d, const mtgl_raster_state *rs)
@@ -114,6 +116,8 @@ uint32_t push_raster(mtgl_dev *d, const mtgl_raster_state *rs)
         R.mip1 = t->mip1;
         R.mip_w = t->mw;
         R.mip_h = t->mh;
+        R.chain = t->chain_tab;
+        R.chain_levels = (int32_t)t->levels.size();
     }
     R.default_depth_range = (rs->depth_near == 0.0 && rs->depth_far == 1.0) ? 1 : 0;
     R.needs_eye = (rs->lighting && (rs->shade_model == GL_PHONG || rs->lit.two_side)) ? 1 : 0;
@@ -370,6 +374,39 @@ int mtgl_dev_buffer_destroy(mtgl_dev *d, mtgl_handle h)
     return MTGL_OK;
 }
 
+// MTGL_OPT_MIPMAP_CHAIN: levels 2.. of t, each the 2x2 box filter of the one before (the
+// kernel that builds level 1), while both sides of the previous level are at least 2.
+static int build_chain(mtgl_dev *d, DevTextureObj *t)
+{
+    cudaStream_t s = d->x.stream;
+    std::vector<DevMip> lv;
+    size_t texels = 0;
+    for (int32_t w = t->mw, h = t->mh; w >= 2 && h >= 2; w /= 2, h /= 2) {
+        lv.push_back(DevMip{nullptr, w / 2, h / 2});
+        texels += (size_t)(w / 2) * (size_t)(h / 2);
+    }
+    if (lv.empty()) return MTGL_OK;
+    CK(cudaMallocAsync((void **)&t->chain, texels * 4, s));
+    CK(cudaMallocAsync((void **)&t->chain_tab, lv.size() * sizeof(DevMip), s));
+    size_t at = 0;
+    const uint32_t *prev = t->mip1;
+    int32_t pw = t->mw, ph = t->mh;
+    for (DevMip &m : lv) {
+        m.px = t->chain + at;
+        at += (size_t)m.w * (size_t)m.h;
+        launch_mip1(prev, pw, ph, const_cast<uint32_t *>(m.px), s);
+        d->stats.kernel_launches++;
+        prev = m.px;
+        pw = m.w;
+        ph = m.h;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(t->chain_tab, lv.data(), lv.size() * sizeof(DevMip), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // the table's source is this function's vector
+    t->levels = std::move(lv);
+    return MTGL_OK;
+}
+
 int mtgl_dev_texture_create(mtgl_dev *d, mtgl_handle *out)
 {
     if (!d || !out) return MTGL_ERR_INVALID;
@@ -389,8 +426,13 @@ int mtgl_dev_texture_image(mtgl_dev *d, mtgl_handle h, int32_t w, int32_t hgt, c
     cudaStream_t s = d->x.stream;
     if (t->base) CK(cudaFreeAsync(t->base, s));
     if (t->mip1) CK(cudaFreeAsync(t->mip1, s));
+    if (t->chain) CK(cudaFreeAsync(t->chain, s));
+    if (t->chain_tab) CK(cudaFreeAsync(t->chain_tab, s));
     t->base = nullptr;
     t->mip1 = nullptr;
+    t->chain = nullptr;
+    t->chain_tab = nullptr;
+    t->levels.clear();
     const size_t n = (size_t)w * (size_t)hgt;
     CK(cudaMallocAsync((void **)&t->base, n * 4, s));
     CK(cudaMemcpyAsync(t->base, rgba32, n * 4, cudaMemcpyHostToDevice, s));
@@ -405,6 +447,27 @@ int mtgl_dev_texture_image(mtgl_dev *d, mtgl_handle h, int32_t w, int32_t hgt, c
         CK(cudaGetLastError());
         d->stats.kernel_launches++;
     }
+    if (d->mipmap_chain && t->mip1) return build_chain(d, t);
+    return MTGL_OK;
+}
+
+int mtgl_dev_texture_level(mtgl_dev *d, mtgl_handle h, int32_t level, int32_t w, int32_t hgt, const uint32_t *rgba32)
+{
+    DevTextureObj *t = reinterpret_cast<DevTextureObj *>(h);
+    if (!d || !t || !rgba32 || level < 1) return MTGL_ERR_INVALID;
+    uint32_t *dst = nullptr;
+    if (level == 1 && t->mip1 && w == t->mw && hgt == t->mh) dst = t->mip1;
+    const size_t k = (size_t)level - 2;
+    if (level >= 2 && k < t->levels.size() && w == t->levels[k].w && hgt == t->levels[k].h)
+        dst = const_cast<uint32_t *>(t->levels[k].px);
+    if (!dst || t->levels.empty()) {
+        snprintf(g_err, sizeof(g_err), "texture level %d of %dx%d: no such level in the texture's chain", level, w, hgt);
+        return MTGL_ERR_INVALID;
+    }
+    CK(cudaSetDevice(d->device));
+    int st = flush_if_drawing(d);
+    if (st || (st = mtgl_dev_enter(d))) return st;
+    CK(cudaMemcpyAsync(dst, rgba32, (size_t)w * (size_t)hgt * 4, cudaMemcpyHostToDevice, d->x.stream));
     return MTGL_OK;
 }
 
@@ -417,6 +480,8 @@ int mtgl_dev_texture_destroy(mtgl_dev *d, mtgl_handle h)
     if (st || (st = mtgl_dev_enter(d))) return st;
     if (t->base) CK(cudaFreeAsync(t->base, d->x.stream));
     if (t->mip1) CK(cudaFreeAsync(t->mip1, d->x.stream));
+    if (t->chain) CK(cudaFreeAsync(t->chain, d->x.stream));
+    if (t->chain_tab) CK(cudaFreeAsync(t->chain_tab, d->x.stream));
     delete t;
     return MTGL_OK;
 }
@@ -632,6 +697,10 @@ void *mtgl_dev_stream(mtgl_dev *d) { return d ? (void *)d->x.stream : nullptr; }
 int mtgl_dev_set_option(mtgl_dev *d, int option, int value)
 {
     if (!d) return MTGL_ERR_INVALID;
+    if (option == MTGL_OPT_MIPMAP_CHAIN) {
+        d->mipmap_chain = value != 0;  // applies to texture images given afterwards
+        return MTGL_OK;
+    }
     if (option != MTGL_OPT_DEPTH_REJECTION) return MTGL_ERR_INVALID;
     if (d->depth_rejection != (value != 0)) {
         d->pass.raster_src.clear();  // the next draw pushes a raster state carrying the new value

@@ -136,6 +136,11 @@ enum FragCtl : uint32_t {
     FC_AFFINE_UV = 1u << 5, FC_FOG = 1u << 6, FC_BLEND = 1u << 7, FC_DEFAULT_RANGE = 1u << 8,
     FC_MASK_ALL = 1u << 9, FC_MASK_NONE = 1u << 10, FC_TEXTURE = 1u << 11
 };
+// A texture level beyond 1 (MTGL_OPT_MIPMAP_CHAIN): packed RGBA8 texels, row-major.
+struct DevMip {
+    const uint32_t *px;
+    int32_t w, h;
+};
 struct __align__(16) FragState {
     uint32_t ctl, depth_func, alpha_func, tex_env_mode;
     uint32_t stencil_func;
@@ -153,9 +158,11 @@ struct __align__(16) FragState {
     const uint32_t *tex, *mip1;            // texture: levels 0 and 1 (see DevRaster)
     int32_t tex_w, tex_h, mip_w, mip_h;
     int32_t wrap_s, wrap_t, min_filter, mag_filter;
+    const DevMip *chain;                   // levels 2.. (MTGL_OPT_MIPMAP_CHAIN), or null
+    int32_t chain_levels, pad1;            // how many (0: the reference's two levels)
 };
 
-static_assert(sizeof(FragState) == 160 && offsetof(FragState, stencil_func) == 16 &&
+static_assert(sizeof(FragState) == 176 && offsetof(FragState, chain) == 160 && offsetof(FragState, stencil_func) == 16 &&
                   offsetof(FragState, stencil_fail) == 32 && offsetof(FragState, blend_src) == 48 &&
                   offsetof(FragState, fog_start) == 64 && offsetof(FragState, fog_color) == 80 &&
                   offsetof(FragState, tex_env_color) == 96 && offsetof(FragState, tex) == 112 &&
@@ -169,6 +176,8 @@ struct DevRaster {
     const uint32_t *tex;   // level 0, or null when texturing is off
     const uint32_t *mip1;  // level 1, or null when the reference cannot build it (w or h < 2)
     int32_t tex_w, tex_h, mip_w, mip_h;
+    const DevMip *chain;   // levels 2.. of a texture built under MTGL_OPT_MIPMAP_CHAIN
+    int32_t chain_levels;
     int32_t default_depth_range;
     int32_t needs_eye;     // per-fragment lighting reads eye-space interpolants
     int32_t depth_rejection;  // MTGL_OPT_DEPTH_REJECTION of the context at enqueue
@@ -477,6 +486,37 @@ __device__ __forceinline__ float trunc_f2i_f(float f)
     return f < 0.0f ? -t : t;  // a -0 here only meets u - t, where it acts as +0
 }
 
+// Level d of a texture with a chain (0: base, 1: mip1, 2..: the chain).
+__device__ __forceinline__ TexView chain_level(const FragState &S, int d)
+{
+    if (d == 0) return TexView{ldg_ptr(&S.tex), __ldg(&S.tex_w), __ldg(&S.tex_h)};
+    if (d == 1) return TexView{ldg_ptr(&S.mip1), __ldg(&S.mip_w), __ldg(&S.mip_h)};
+    const DevMip *m = reinterpret_cast<const DevMip *>(__ldg(reinterpret_cast<const unsigned long long *>(&S.chain)));
+    return TexView{ldg_ptr(&m[d - 2].px), __ldg(&m[d - 2].w), __ldg(&m[d - 2].h)};
+}
+
+// The mipmap filters over a whole chain (MTGL_OPT_MIPMAP_CHAIN; no counterpart in the
+// reference): levels 0 .. top, lod > 0. *_MIPMAP_NEAREST takes level floor(lod + 0.5);
+// *_MIPMAP_LINEAR blends levels floor(lod) and floor(lod) + 1 by the fraction, as the
+// reference blends levels 0 and 1 (lerp of the unpacked texels, repacked); from the top
+// level up, that level alone.
+static __device__ __noinline__ uint32_t sample_chain(const FragState &S, int32_t ws, int32_t wt, float u, float v, float lod,
+                                              int32_t filter, int top)
+{
+    const bool lin = filter == GL_LINEAR_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_LINEAR;
+    if (filter == GL_NEAREST_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_NEAREST) {
+        const int d = lod >= (float)top ? top : (int)(lod + 0.5f);
+        return sample_level(chain_level(S, min(d, top)), ws, wt, u, v, lin);
+    }
+    if (lod >= (float)top) return sample_level(chain_level(S, top), ws, wt, u, v, lin);
+    const int d = (int)lod;
+    const float t = lod - (float)d;
+    const uint32_t c0 = sample_level(chain_level(S, d), ws, wt, u, v, lin);
+    const uint32_t c1 = sample_level(chain_level(S, d + 1), ws, wt, u, v, lin);
+    const float4 r = lerp_col(unpack_rgba(c0), unpack_rgba(c1), t);
+    return pack_rgba(r.x, r.y, r.z, r.w);
+}
+
 // texture_sample_lod (textures.c:457-557) on the packed texture state
 __device__ inline uint32_t sample_lod(const FragState &S, float u, float v, float lod)
 {
@@ -497,6 +537,10 @@ __device__ inline uint32_t sample_lod(const FragState &S, float u, float v, floa
         if (v > 1.0f) v = 1.0f;
     }
     int32_t filter = (lod > 0.0f) ? mode.z : mode.w;
+    if (lod > 0.0f && filter != GL_NEAREST && filter != GL_LINEAR) {
+        const int chain = __ldg(&S.chain_levels);
+        if (chain > 0) return sample_chain(S, ws, wt, u, v, lod, filter, 1 + chain);
+    }
     if (filter == GL_NEAREST_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_NEAREST) {
         if (lod >= 0.5f) return sample_mip1(S, ws, wt, u, v, filter);
         filter = (filter == GL_NEAREST_MIPMAP_NEAREST) ? GL_NEAREST : GL_LINEAR;

@@ -182,7 +182,10 @@ int mtgl_get_timings(GLState *c, mtgl_timings *out) { return c ? mtgl_dev_timing
 void *mtgl_cuda_stream(GLState *c) { return c ? mtgl_dev_stream(c->dev) : NULL; }
 int mtgl_set_option(GLState *c, int option, int value)
 {
-    return c ? mtgl_dev_set_option(c->dev, option, value) : MTGL_ERR_INVALID;
+    if (!c) return MTGL_ERR_INVALID;
+    int st = mtgl_dev_set_option(c->dev, option, value);
+    if (st == MTGL_OK && option == MTGL_OPT_MIPMAP_CHAIN) c->mipmap_chain = value != 0;
+    return st;
 }
 
 /* the back end of a context, for back-end entry points that take a GLState (not exported) */

@@ -134,6 +134,7 @@ typedef struct {
 struct GLState {
     mtgl_dev *dev;
     int32_t width, height;
+    int mipmap_chain; /* MTGL_OPT_MIPMAP_CHAIN: glTexImage2D accepts levels above 0 */
 
     float clear_color[4];
     double clear_depth;

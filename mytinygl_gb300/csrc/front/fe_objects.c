@@ -108,7 +108,10 @@ void glBindTexture(GLenum target, GLuint id)
 }
 
 /* glTexImage2D (gl_api.c:794-834) + texture_upload_* (textures.c:141-269): level 0 only;
- * every format becomes packed RGBA8 (graphics.h:420-434). */
+ * every format becomes packed RGBA8 (graphics.h:420-434). Under the MTGL_OPT_MIPMAP_CHAIN
+ * extension (no counterpart in the reference) a level above 0 of an uploaded texture
+ * replaces that level of its chain: GL_INVALID_OPERATION without a level-0 image,
+ * GL_INVALID_VALUE when the chain has no such level or the size is not the level's. */
 void glTexImage2D(GLenum target, GLint level, GLint internalformat, GLsizei width, GLsizei height, GLint border,
                   GLenum format, GLenum type, const GLvoid *pixels)
 {
@@ -120,7 +123,7 @@ void glTexImage2D(GLenum target, GLint level, GLint internalformat, GLsizei widt
         fe_set_error(c, GL_INVALID_ENUM);
         return;
     }
-    if (level != 0 || type != GL_UNSIGNED_BYTE) {
+    if ((level != 0 && !(c->mipmap_chain && level > 0)) || type != GL_UNSIGNED_BYTE) {
         fe_set_error(c, GL_INVALID_VALUE);
         return;
     }
@@ -157,6 +160,18 @@ void glTexImage2D(GLenum target, GLint level, GLint internalformat, GLsizei widt
         texels[i] = (a << 24) | (b << 16) | (g << 8) | r;
     }
     int st = MTGL_OK;
+    if (level > 0) {
+        if (!t->has_image || !t->dev) {
+            free(texels);
+            fe_set_error(c, GL_INVALID_OPERATION);
+            return;
+        }
+        st = mtgl_dev_texture_level(c->dev, t->dev, level, width, height, texels);
+        free(texels);
+        if (st == MTGL_ERR_INVALID) fe_set_error(c, GL_INVALID_VALUE);
+        else if (st != MTGL_OK) fe_dev_error(c, st);
+        return;
+    }
     if (!t->dev) st = mtgl_dev_texture_create(c->dev, &t->dev);
     if (st == MTGL_OK) st = mtgl_dev_texture_image(c->dev, t->dev, width, height, texels);
     free(texels);

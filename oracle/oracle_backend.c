@@ -175,11 +175,16 @@ typedef struct {
     uint64_t size;
 } obuf;
 
+#define OMAX_CHAIN 16
 typedef struct {
     int32_t width, height;
     uint32_t *pixels;
     int32_t mip1_width, mip1_height;
     uint32_t *mip1;
+    /* MTGL_OPT_MIPMAP_CHAIN (an extension of this library, not of the reference): levels 2.. */
+    int nchain;
+    int32_t chain_w[OMAX_CHAIN], chain_h[OMAX_CHAIN];
+    uint32_t *chain[OMAX_CHAIN];
 } otex;
 
 struct mtgl_dev {
@@ -189,6 +194,7 @@ struct mtgl_dev {
     uint8_t *stencil;
     mtgl_stats stats;
     const mtgl_raster_state *rs; /* raster state of the packet being rendered */
+    int mipmap_chain;            /* MTGL_OPT_MIPMAP_CHAIN */
 };
 
 const char *mtgl_dev_last_error(void) { return ""; }
@@ -272,10 +278,18 @@ int mtgl_dev_texture_create(mtgl_dev *d, mtgl_handle *out)
     return MTGL_OK;
 }
 
+static void free_chain(otex *t)
+{
+    for (int i = 0; i < t->nchain; i++) free(t->chain[i]);
+    t->nchain = 0;
+}
+
+static int gen_mip1(otex *t);
+static int build_chain(otex *t);
+
 /* texture_upload_* (textures.c:141-174): new base level, mip level 1 invalidated */
 int mtgl_dev_texture_image(mtgl_dev *d, mtgl_handle h, int32_t width, int32_t height, const uint32_t *rgba32)
 {
-    (void)d;
     otex *t = (otex *)(uintptr_t)h;
     if (!t || width <= 0 || height <= 0) return MTGL_ERR_INVALID;
     size_t n = (size_t)width * (size_t)height;
@@ -284,11 +298,29 @@ int mtgl_dev_texture_image(mtgl_dev *d, mtgl_handle h, int32_t width, int32_t he
     memcpy(p, rgba32, n * 4);
     free(t->pixels);
     free(t->mip1);
+    free_chain(t);
     t->mip1 = NULL;
     t->mip1_width = t->mip1_height = 0;
     t->pixels = p;
     t->width = width;
     t->height = height;
+    /* the extension builds every level at once (level 1 as the reference builds it) */
+    if (d && d->mipmap_chain && gen_mip1(t) == 0 && build_chain(t) != 0) return MTGL_ERR_OOM;
+    return MTGL_OK;
+}
+
+int mtgl_dev_texture_level(mtgl_dev *d, mtgl_handle h, int32_t level, int32_t width, int32_t height,
+                           const uint32_t *rgba32)
+{
+    (void)d;
+    otex *t = (otex *)(uintptr_t)h;
+    if (!t || !rgba32 || level < 1 || t->nchain == 0) return MTGL_ERR_INVALID;
+    uint32_t *dst = NULL;
+    if (level == 1 && t->mip1 && width == t->mip1_width && height == t->mip1_height) dst = t->mip1;
+    if (level >= 2 && level - 2 < t->nchain && width == t->chain_w[level - 2] && height == t->chain_h[level - 2])
+        dst = t->chain[level - 2];
+    if (!dst) return MTGL_ERR_INVALID;
+    memcpy(dst, rgba32, (size_t)width * (size_t)height * 4);
     return MTGL_OK;
 }
 
@@ -299,6 +331,7 @@ int mtgl_dev_texture_destroy(mtgl_dev *d, mtgl_handle h)
     if (!t) return MTGL_OK;
     free(t->pixels);
     free(t->mip1);
+    free_chain(t);
     free(t);
     return MTGL_OK;
 }
@@ -516,10 +549,19 @@ static col compute_lighting(const mtgl_lighting *L, v3 eye_pos, v3 eye_normal, c
 
 /* ------------------------------------------------------------------ textures (textures.c:271-563) */
 
+/* level `mip` of a texture: 0 the base, 1 the reference's level 1, 2.. the extension's chain */
+static void level_of(const otex *t, int mip, const uint32_t **px, int32_t *w, int32_t *h)
+{
+    if (mip == 0) { *px = t->pixels; *w = t->width; *h = t->height; }
+    else if (mip == 1) { *px = t->mip1; *w = t->mip1_width; *h = t->mip1_height; }
+    else { *px = t->chain[mip - 2]; *w = t->chain_w[mip - 2]; *h = t->chain_h[mip - 2]; }
+}
+
 static uint32_t texel_wrapped(const otex *t, const mtgl_raster_state *rs, int32_t x, int32_t y, int mip)
 {
-    int32_t w = mip ? t->mip1_width : t->width, h = mip ? t->mip1_height : t->height;
-    const uint32_t *px = mip ? t->mip1 : t->pixels;
+    const uint32_t *px;
+    int32_t w, h;
+    level_of(t, mip, &px, &w, &h);
     if (rs->tex_wrap_s == GL_REPEAT) x = ((x % w) + w) % w;
     else { if (x < 0) x = 0; else if (x >= w) x = w - 1; }
     if (rs->tex_wrap_t == GL_REPEAT) y = ((y % h) + h) % h;
@@ -559,9 +601,42 @@ static int gen_mip1(otex *t)
     return 0;
 }
 
+/* the extension's levels 2..: the 2x2 box filter of texture_generate_mip1 (textures.c:311-354)
+ * applied to each level in turn, while both sides of the previous one are at least 2 */
+static int build_chain(otex *t)
+{
+    const uint32_t *src = t->mip1;
+    int32_t sw = t->mip1_width, sh = t->mip1_height;
+    while (sw >= 2 && sh >= 2 && t->nchain < OMAX_CHAIN) {
+        int32_t w = sw / 2, h = sh / 2;
+        uint32_t *dst = (uint32_t *)malloc((size_t)w * h * 4);
+        if (!dst) return -1;
+        for (int32_t y = 0; y < h; y++)
+            for (int32_t x = 0; x < w; x++) {
+                int32_t sx = 2 * x, sy = 2 * y;
+                col c = c_from_rgba32(src[(size_t)sy * sw + sx]);
+                c = c_add(c, c_from_rgba32(src[(size_t)sy * sw + sx + 1]));
+                c = c_add(c, c_from_rgba32(src[(size_t)(sy + 1) * sw + sx]));
+                c = c_add(c, c_from_rgba32(src[(size_t)(sy + 1) * sw + sx + 1]));
+                c = c_scale(c, 0.25f);
+                dst[(size_t)y * w + x] = c_to_rgba32(c);
+            }
+        t->chain[t->nchain] = dst;
+        t->chain_w[t->nchain] = w;
+        t->chain_h[t->nchain] = h;
+        t->nchain++;
+        src = dst;
+        sw = w;
+        sh = h;
+    }
+    return 0;
+}
+
 static uint32_t sample_level(otex *t, const mtgl_raster_state *rs, float u, float v, int linear, int mip)
 {
-    int32_t w = mip ? t->mip1_width : t->width, h = mip ? t->mip1_height : t->height;
+    const uint32_t *lpx;
+    int32_t w, h;
+    level_of(t, mip, &lpx, &w, &h);
     float tx = u * w - 0.5f;
     float ty = v * h - 0.5f;
     if (linear) {
@@ -576,7 +651,28 @@ static uint32_t sample_level(otex *t, const mtgl_raster_state *rs, float u, floa
     if (x >= w) x = w - 1;
     if (y < 0) y = 0;
     if (y >= h) y = h - 1;
-    return (mip ? t->mip1 : t->pixels)[(size_t)y * w + x];
+    return lpx[(size_t)y * w + x];
+}
+
+/* The extension's mipmap filters over the whole chain (levels 0 .. top, lod > 0):
+ * *_MIPMAP_NEAREST the level floor(lod + 0.5), *_MIPMAP_LINEAR the blend of levels floor(lod)
+ * and floor(lod) + 1 by the fraction, as the reference blends levels 0 and 1; from the top
+ * level up, that level alone. */
+static uint32_t sample_chain(otex *t, const mtgl_raster_state *rs, float u, float v, float lod, int32_t filter)
+{
+    int top = 1 + t->nchain;
+    int lin = filter == GL_LINEAR_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_LINEAR;
+    if (filter == GL_NEAREST_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_NEAREST) {
+        int d = lod >= (float)top ? top : (int)(lod + 0.5f);
+        if (d > top) d = top;
+        return sample_level(t, rs, u, v, lin, d);
+    }
+    if (lod >= (float)top) return sample_level(t, rs, u, v, lin, top);
+    int d = (int)lod;
+    float f = lod - (float)d;
+    uint32_t c0 = sample_level(t, rs, u, v, lin, d);
+    uint32_t c1 = sample_level(t, rs, u, v, lin, d + 1);
+    return c_to_rgba32(c_lerp(c_from_rgba32(c0), c_from_rgba32(c1), f));
 }
 
 static uint32_t sample_mip1(otex *t, const mtgl_raster_state *rs, float u, float v, int32_t filter)
@@ -605,6 +701,8 @@ static uint32_t sample_lod(otex *t, const mtgl_raster_state *rs, float u, float 
         if (v > 1.0f) v = 1.0f;
     }
     int32_t filter = (lod > 0.0f) ? rs->tex_min_filter : rs->tex_mag_filter;
+    if (lod > 0.0f && filter != GL_NEAREST && filter != GL_LINEAR && t->nchain > 0)
+        return sample_chain(t, rs, u, v, lod, filter);
     if (filter == GL_NEAREST_MIPMAP_NEAREST || filter == GL_LINEAR_MIPMAP_NEAREST) {
         if (lod >= 0.5f) return sample_mip1(t, rs, u, v, filter);
         filter = (filter == GL_NEAREST_MIPMAP_NEAREST) ? GL_NEAREST : GL_LINEAR;
@@ -1404,8 +1502,10 @@ int mtgl_flush_noalloc(GLState *ctx)
 
 int mtgl_dev_set_option(mtgl_dev *d, int option, int value)
 {
-    (void)d;
-    (void)value;
+    if (option == MTGL_OPT_MIPMAP_CHAIN) {
+        if (d) d->mipmap_chain = value != 0;
+        return MTGL_OK;
+    }
     return option == MTGL_OPT_DEPTH_REJECTION ? MTGL_OK : MTGL_ERR_INVALID;
 }
 

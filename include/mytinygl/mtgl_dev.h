@@ -152,6 +152,8 @@ typedef struct {
                                       passes (scratch, staging areas) */
     uint64_t vertices;             /* vertex slots transformed by the vertex stage */
     uint64_t vertex_bytes;         /* attribute bytes those slots read (enabled arrays) */
+    uint64_t debug_status;         /* build with MTGL_DEBUG_BOUNDS: the site code of the first
+                                      device index check that failed (0: none); else 0 */
 } mtgl_stats;
 
 /* Device time per pipeline phase, summed over the passes since profiling was enabled
@@ -202,6 +204,11 @@ int mtgl_dev_in_batch(const mtgl_dev *d);
 /* Finish, then copy whole buffers (row 0 = top) to host memory; any pointer may be NULL. */
 int mtgl_dev_read(mtgl_dev *d, uint32_t *color, float *depth, uint8_t *stencil);
 int mtgl_dev_stats(mtgl_dev *d, mtgl_stats *out);
+/* 1 in a build with MTGL_DEBUG_BOUNDS (device index checks that record a failing site in
+ * mtgl_stats.debug_status and skip the access, never trapping), else 0. No counterpart in
+ * the reference, whose framebuffer accessors can only have their checks removed
+ * (framebuffer.h:92-163). */
+int mtgl_dev_debug_bounds(void);
 int mtgl_dev_reset_stats(mtgl_dev *d);
 /* Per-phase device timing (off by default); enabling resets the sums. */
 int mtgl_dev_profile(mtgl_dev *d, int enable);
@@ -259,6 +266,7 @@ typedef struct {
     uint32_t record_capacity, pair_capacity;
     int32_t tile_size, ctas;
     uint64_t vertices, vertex_bytes; /* as in mtgl_stats, over the batch's passes */
+    uint64_t debug_status;           /* as in mtgl_stats */
 } mtgl_batch_stats;
 
 /* The defaults mtgl_dev_batch_create uses for zero fields. */

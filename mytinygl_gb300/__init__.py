@@ -11,15 +11,17 @@ from . import build as _build
 LIB_PATH = _build.LIB_PATH
 
 
-def build(verbose=False, force=False) -> str:
-    return _build.build(verbose=verbose, force=force)
+def build(verbose=False, force=False, debug_bounds=False) -> str:
+    return _build.build(verbose=verbose, force=force, debug_bounds=debug_bounds)
 
 
-def library():
-    """Load libmytinygl_gb300.so. There is no CPU fallback: a missing library is an error,
+def library(debug_bounds=False):
+    """Load libmytinygl_gb300.so (debug_bounds: libmytinygl_gb300_debug.so, the build whose
+    kernels check their indices). There is no CPU fallback: a missing library is an error,
     and creating a context without a visible CUDA device fails."""
     from . import gl
 
-    if not os.path.exists(LIB_PATH):
-        raise RuntimeError(f"{LIB_PATH} is not built; run mytinygl_gb300.build() (nvcc, sm_103a)")
-    return gl.load(LIB_PATH)
+    path = _build.DEBUG_LIB_PATH if debug_bounds else LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is not built; run mytinygl_gb300.build() (nvcc, sm_103a)")
+    return gl.load(path)

@@ -5,7 +5,9 @@ Kernels:   nvcc for sm_103a only, -fmad=false with IEEE division and square root
            float operation rounds as the reference's does on x86-64.
 Translation units compile in parallel; an object is rebuilt when any source or header is
 newer. The library is built in-tree (mytinygl_gb300/lib/) and links the CUDA runtime
-statically.
+statically. build(debug_bounds=True) builds libmytinygl_gb300_debug.so instead, with
+MTGL_DEBUG_BOUNDS defined: the kernels check the indices of their data-dependent accesses
+and record a failing site in mtgl_stats.debug_status instead of making the access.
 """
 from __future__ import annotations
 
@@ -25,6 +27,8 @@ SERVE_DIR = os.path.join(PKG, "csrc", "serve")
 LIB_DIR = os.path.join(PKG, "lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libmytinygl_gb300.so")
+DEBUG_OBJ_DIR = os.path.join(LIB_DIR, "obj_debug")
+DEBUG_LIB_PATH = os.path.join(LIB_DIR, "libmytinygl_gb300_debug.so")
 EXPORTS = os.path.join(PKG, "csrc", "exports.map")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -63,36 +67,38 @@ def _run(cmd, log):
     return r
 
 
-def build(verbose=False, force=False) -> str:
-    os.makedirs(OBJ_DIR, exist_ok=True)
+def build(verbose=False, force=False, debug_bounds=False) -> str:
+    obj_dir, lib_path = (DEBUG_OBJ_DIR, DEBUG_LIB_PATH) if debug_bounds else (OBJ_DIR, LIB_PATH)
+    extra = ["-DMTGL_DEBUG_BOUNDS"] if debug_bounds else []
+    os.makedirs(obj_dir, exist_ok=True)
     nvcc = nvcc_path()
     headers = _headers()
     jobs = []
     objs = []
     for src in sorted(glob.glob(os.path.join(DEV_DIR, "*.cu"))):
-        obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, src, headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc] + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
     for src in sorted(glob.glob(os.path.join(FRONT_DIR, "*.c")) + glob.glob(os.path.join(SERVE_DIR, "*.c"))):
-        obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, src, headers):
-            jobs.append(["gcc"] + CC_FLAGS + ["-pthread", "-c", src, "-o", obj])
+            jobs.append(["gcc"] + CC_FLAGS + extra + ["-pthread", "-c", src, "-o", obj])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             futs = [ex.submit(_run, j, j[-1] + ".log") for j in jobs]
             for f in futs:
                 f.result()
-    if force or jobs or not os.path.exists(LIB_PATH):
-        tmp = LIB_PATH + ".tmp"
+    if force or jobs or not os.path.exists(lib_path):
+        tmp = lib_path + ".tmp"
         _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs +
              ["-Xlinker", "-Bsymbolic", "-Xlinker", "--exclude-libs,ALL", "-Xlinker",
-              f"--version-script={EXPORTS}", "-lm", "-lpthread"], os.path.join(OBJ_DIR, "link.log"))
-        os.replace(tmp, LIB_PATH)
+              f"--version-script={EXPORTS}", "-lm", "-lpthread"], os.path.join(obj_dir, "link.log"))
+        os.replace(tmp, lib_path)
     if verbose:
-        print(f"built {LIB_PATH} ({len(jobs)} objects rebuilt)")
-    return LIB_PATH
+        print(f"built {lib_path} ({len(jobs)} objects rebuilt)")
+    return lib_path
 
 
 def ptxas_report() -> str:

@@ -550,6 +550,9 @@ int mtgl_dev_batch_stats(mtgl_batch *b, mtgl_batch_stats *out)
     CK(cudaStreamSynchronize(b->x.stream));
     *out = b->stats;
     out->fragments = f;
+    uint32_t dbg = 0;
+    CK(cudaMemcpy(&dbg, b->x.d_totals + kDebugStatusWord, sizeof(dbg), cudaMemcpyDeviceToHost));
+    out->debug_status = dbg;
     return MTGL_OK;
 }
 
@@ -563,6 +566,7 @@ int mtgl_dev_batch_reset_stats(mtgl_batch *b)
     b->stats.tile_size = ts;
     b->stats.ctas = ctas;
     CK(cudaMemsetAsync(b->x.d_frags, 0, sizeof(unsigned long long), b->x.stream));
+    CK(cudaMemsetAsync(b->x.d_totals + kDebugStatusWord, 0, sizeof(uint32_t), b->x.stream));
     CK(cudaStreamSynchronize(b->x.stream));
     return MTGL_OK;
 }

@@ -12,6 +12,7 @@ constexpr uint32_t kClipClasses = 96;  // one-plane candidates: first plane x in
 // Each class is counted in kClipSlots counters (a block of the count pass uses slot
 // blockIdx % kClipSlots), so that the appends of many blocks do not all meet on a few words.
 constexpr uint32_t kClipSlots = 32;
+constexpr int kDebugStatusWord = 8;  // word of an Exec's counters that the debug bounds checks write
 constexpr uint32_t kClipBuckets = kClipClasses * kClipSlots;  // class-major
 
 struct GeomArgs {
@@ -38,6 +39,7 @@ struct GeomArgs {
     uint32_t *class_count;            // kClipBuckets counters (zeroed by the count launch)
     uint32_t *clip_count;             // their number (device; zeroed by the count launch)
     int32_t sms;
+    uint32_t *debug;                  // status word of the debug bounds checks
 };
 
 // K1: per-vertex stage (gl_api.c:263-348) for every vertex slot of the pass.
@@ -77,6 +79,7 @@ struct BinArgs {
     uint32_t *sort_total_dev;   // a word the sort's histogram scans may overwrite
     uint32_t npairs;            // pair capacity of keys/vals (writes beyond are dropped)
     int32_t sms;                // SMs of the device (grid sizes)
+    uint32_t *debug;            // status word of the debug bounds checks
 };
 
 int launch_bin_count(const BinArgs &a, cudaStream_t s);
@@ -138,6 +141,8 @@ struct TileArgs {
     uint32_t records_cap, pairs_cap;
     unsigned long long *fragments;
     int32_t defer;               // every record is a filled triangle with deferrable colour (k_tile.cuh)
+    uint32_t *debug;             // status word of the debug bounds checks
+    uint32_t entries_cap;        // entries tile_vals holds (debug bounds checks)
 };
 
 // K4: CTAs take tiles from the work queue; for each: clears, then every triangle of the

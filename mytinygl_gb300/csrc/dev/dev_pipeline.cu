@@ -516,6 +516,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ga.clip_sorted = tris < (1u << 24) ? clip_list + 2 * (size_t)tris : nullptr;
     ga.class_count = clip_list + 3 * (size_t)tris;
     ga.clip_count = x.d_totals + 4;
+    ga.debug = x.d_totals + kDebugStatusWord;
     ga.sms = x.sms;
     int launches = 0;
     launches += launch_vertex(ga, s);
@@ -561,6 +562,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ba.tile_start = tile_start;
     ba.total_dev = x.d_totals + 1;
     ba.sort_total_dev = x.d_totals + 3;
+    ba.debug = x.d_totals + kDebugStatusWord;
     ba.scan_temp = scan_temp;
     ba.sms = x.sms;
     uint32_t pair_cap = c.pair_cap;
@@ -601,6 +603,9 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ta.eye_records = eye_records;
     ta.tile_vals = rec_cap ? ba.vals : nullptr;
     ta.pair_mask = rec_cap ? ba.keys : nullptr;
+    ta.debug = x.d_totals + kDebugStatusWord;
+    ta.records_cap = rec_cap;
+    ta.entries_cap = rec_cap ? pair_cap : 0u;
     ta.tile_start = tile_start;
     ta.tile_count = tile_count;
     ta.rasters = ga.rasters;
@@ -627,7 +632,6 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     }
     if (!c.exact) {
         ta.guard = x.d_totals;
-        ta.records_cap = rec_cap;
         ta.pairs_cap = pair_cap;
     }
     launches += launch_tile(ta, s);

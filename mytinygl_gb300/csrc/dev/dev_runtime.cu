@@ -668,6 +668,9 @@ int mtgl_dev_stats(mtgl_dev *d, mtgl_stats *out)
     *out = d->stats;
     out->fragments = f;
     out->allocations = d->x.pool.allocs + d->x.allocs + d->stage.allocs - d->alloc_base;
+    uint32_t dbg = 0;
+    CK(cudaMemcpy(&dbg, d->x.d_totals + kDebugStatusWord, sizeof(dbg), cudaMemcpyDeviceToHost));
+    out->debug_status = dbg;
     return MTGL_OK;
 }
 
@@ -717,8 +720,18 @@ int mtgl_dev_reset_stats(mtgl_dev *d)
     memset(&d->stats, 0, sizeof(d->stats));
     d->alloc_base = d->x.pool.allocs + d->x.allocs + d->stage.allocs;
     CK(cudaMemsetAsync(d->x.d_frags, 0, sizeof(unsigned long long), d->x.stream));
+    CK(cudaMemsetAsync(d->x.d_totals + kDebugStatusWord, 0, sizeof(uint32_t), d->x.stream));
     CK(cudaStreamSynchronize(d->x.stream));
     return MTGL_OK;
+}
+
+int mtgl_dev_debug_bounds(void)
+{
+#ifdef MTGL_DEBUG_BOUNDS
+    return 1;
+#else
+    return 0;
+#endif
 }
 
 }  // extern "C"

@@ -295,6 +295,7 @@ __global__ void __launch_bounds__(256) k_tile_bounds(BinArgs A)
     const uint32_t n = min(*A.total_dev, A.npairs);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t k = A.keys[i];
+        if (!debug_check(A.debug, k < A.ntiles, DBG_BIN_TILE)) continue;
         if (i == 0 || A.keys[i - 1] != k) A.tile_start[k] = i;
         if (i + 1 == n || A.keys[i + 1] != k) A.tile_count[k] = i + 1;
     }

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(128) k_vertex(GeomArgs A)
     o.uv = uv;
     o.eye_z = -eye.z;
     o.pad = 0.0f;
+    if (!debug_check(A.debug, g < A.total_slots, DBG_VERTEX_SLOT)) return;
     A.verts[g] = o;
     if (A.eyes) {
         PostEye e;
@@ -791,7 +792,7 @@ struct RecOut {
     uint32_t base, cap;
     __device__ float *rec(uint32_t i) const
     {
-        return (recs && base + i < cap) ? recs + (size_t)(base + i) * kRecWords : nullptr;
+        return (recs && base + i < cap) ? recs + (size_t)(base + i) * kRecWords : nullptr;  // beyond: dropped
     }
     __device__ float *eye(uint32_t i) const
     {

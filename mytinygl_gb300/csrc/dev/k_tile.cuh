@@ -541,8 +541,13 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
         // walks the list on its own, 32 entries per step, taking those whose mask names its
         // block: no barrier between warps, which differ in how much work their blocks hold.
         const float4 *recs4 = reinterpret_cast<const float4 *>(A.records);
+        if (!debug_check(A.debug, (uint64_t)start + count <= A.entries_cap, DBG_TILE_ENTRY)) continue;
         for (uint32_t i = threadIdx.x; i < count; i += TS * TS) {
             const uint32_t idx = __ldg(A.tile_vals + start + i);
+            if (!debug_check(A.debug, idx < A.records_cap, DBG_TILE_RECORD)) {
+                A.pair_mask[start + i] = 0u;
+                continue;
+            }
             const float4 *q = recs4 + (size_t)idx * (kRecWords / 4);
             const float4 bb = __ldg(q + 1), bb2 = __ldg(q + 2), q12 = __ldg(q + 12);
             A.pair_mask[start + i] = block_mask<TS>(q, bb, bb2, q12, __float_as_uint(q12.x), tx * TS, ty * TS,
@@ -637,7 +642,7 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
         }
 
         if (DEFER && pend != kNoPending) col = pending_color<TEX, EYE>(A, pend, have_eye, fpx, fpy);
-        if (in_fb) {
+        if (in_fb && debug_check(A.debug, pix < (size_t)F.dims.width * (size_t)F.dims.height, DBG_TILE_PIXEL)) {
             F.color[pix] = col;
             F.depth[pix] = dep;
             F.stencil[pix] = (uint8_t)st;

@@ -15,6 +15,35 @@
 
 namespace mtgl {
 
+// ------------------------------------------------------------------ debug bounds checks
+//
+// A build with MTGL_DEBUG_BOUNDS defined (mytinygl_gb300.build(debug_bounds=True)) checks the
+// index of every device-memory access the kernels compute from data (framebuffer pixels,
+// triangle records, tile-list entries, tile ids, vertex slots). A failed check never traps:
+// it records its site code in the context's status word (the first failure wins; read back
+// through mtgl_stats.debug_status) and skips the access. In the ordinary build the checks
+// compile to nothing.
+enum DebugSite : uint32_t {
+    DBG_TILE_PIXEL = 1,    // K4: framebuffer pixel index
+    DBG_TILE_RECORD = 2,   // K4: record index from a tile list
+    DBG_TILE_ENTRY = 3,    // K4: tile-list position
+    DBG_BIN_TILE = 4,      // binning: tile id of a sorted pair
+    DBG_VERTEX_SLOT = 5,   // K1: vertex slot
+    DBG_SETUP_RECORD = 6,  // K2: record position
+};
+__device__ __forceinline__ bool debug_check(uint32_t *status, bool ok, uint32_t site)
+{
+#ifdef MTGL_DEBUG_BOUNDS
+    if (!ok && status) atomicCAS(status, 0u, site);
+    return ok;
+#else
+    (void)status;
+    (void)site;
+    (void)ok;
+    return true;
+#endif
+}
+
 // ------------------------------------------------------------------ layout constants
 
 constexpr int kTileShiftMin = 3;     // tile edges of 8, 16 or 32 pixels (one CTA per tile)

@@ -90,7 +90,7 @@ class Stats(ctypes.Structure):
     """mtgl_stats (include/mytinygl/mtgl_dev.h)"""
     _fields_ = [(n, ctypes.c_uint64) for n in ("draws", "input_triangles", "setup_triangles", "bin_entries",
                                                "fragments", "passes", "kernel_launches", "staged_bytes",
-                                               "allocations", "vertices", "vertex_bytes")]
+                                               "allocations", "vertices", "vertex_bytes", "debug_status")]
 
 
 class BatchConfig(ctypes.Structure):
@@ -107,7 +107,8 @@ class BatchStats(ctypes.Structure):
                                                "overflow_reruns", "kernel_launches")] + \
                [("record_capacity", ctypes.c_uint32), ("pair_capacity", ctypes.c_uint32),
                 ("tile_size", ctypes.c_int32), ("ctas", ctypes.c_int32),
-                ("vertices", ctypes.c_uint64), ("vertex_bytes", ctypes.c_uint64)]
+                ("vertices", ctypes.c_uint64), ("vertex_bytes", ctypes.c_uint64),
+                ("debug_status", ctypes.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -1500,6 +1500,8 @@ int mtgl_flush_noalloc(GLState *ctx)
     return ctx ? MTGL_OK : MTGL_ERR_INVALID;
 }
 
+int mtgl_dev_debug_bounds(void) { return 0; }
+
 int mtgl_dev_set_option(mtgl_dev *d, int option, int value)
 {
     if (option == MTGL_OPT_MIPMAP_CHAIN) {

@@ -543,7 +543,7 @@ def batch_config(spec, scenes, world):
 
 
 def serve_config(spec, args, requests, world):
-    return {"workload": spec["name"], "description": spec["desc"], "offered_rate": 2000.0,
+    return {"workload": spec["name"], "description": spec["desc"], "offered_rate": args.serve_rate,
             "duration_s": args.serve_seconds, "requests": requests, "memory_budget_gib": 40,
             "parallelism": f"replicas x{world}"}
 
@@ -833,7 +833,7 @@ def run_serve(args, spec):
         c.glFinish()
         ctxs.append(c)
         srv.add_scene(c, sc.stream(k), W.scene_triangles(sc))
-    rate = 2000.0
+    rate = args.serve_rate
     # warm-up: capacities learned, graphs captured, framebuffer pool filled
     for i in range(args.warmup):
         warm = W.serve_trace(0.5, rate, seed=100 + i)
@@ -1168,7 +1168,7 @@ def run_reference(args, spec):
         desc = (f"{len(times)} requests of the trace in order, each frame rendered on its own oracle context "
                 f"(scene set-up untimed), {threads} threads at once; frames/s = threads / mean frame time")
         return line(fps, statistics.mean(times) * 1e3,
-                    serve_config(spec, args, len(W.serve_trace(args.serve_seconds, 2000.0, seed=6)), world),
+                    serve_config(spec, args, len(W.serve_trace(args.serve_seconds, args.serve_rate, seed=6)), world),
                     "synthetic (seeded; mytinygl_gb300/workloads.py serve_scenes / serve_trace)", desc,
                     latency_ms={"p50": round(float(np.percentile(times, 50)) * 1e3, 3),
                                 "p99": round(float(np.percentile(times, 99)) * 1e3, 3)})
@@ -1223,6 +1223,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle comparison of the timed frames")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving trace length (workload serve)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (workload serve)")
     ap.add_argument("--frames", type=int, default=256, help="frames per step of the batch workload")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least three untimed warm-up steps

@@ -100,7 +100,7 @@ struct Pass {
 enum ScratchSlot {
     S_VERTS, S_EYES, S_TRI_COUNTS, S_TRI_OFFSETS, S_RECORDS, S_EYE_RECORDS, S_REC_TILES, S_KEYS, S_VALS,
     S_KEYS_ALT, S_VALS_ALT, S_TILE_COUNT, S_TILE_START, S_RADIX_HIST, S_SCAN_TEMP, S_ORDER, S_ORDER_AUX,
-    S_CLIP_LIST, kScratchSlots
+    S_CLIP_LIST, S_TILE_FRAME, kScratchSlots
 };
 
 struct ScratchSource {

@@ -73,6 +73,7 @@ struct BinArgs {
     uint32_t *tile_count;       // per tile (ntiles + 1 entries)
     uint32_t *tile_area;        // per tile: pixels of its records' boxes inside it, summed (may be null)
     uint32_t *tile_start;       // exclusive scan of tile_count
+    uint32_t *tile_frame;       // per tile: the frame owning it (written by the range pass; may be null)
     uint32_t *radix_hist;       // radix histograms
     uint32_t *scan_temp;
     uint32_t *total_dev;        // where the pair scan writes its total: the pairs generated
@@ -121,6 +122,7 @@ struct TileArgs {
                                  // by the tile's CTA; binning's sorted keys, no longer read)
     const uint32_t *tile_start;  // per tile
     const uint32_t *tile_count;
+    const uint32_t *tile_frame;  // per tile: its frame (null: found by a search of the frame table)
     const DevRaster *rasters;
     uint32_t nrasters;
     const ClearOp *clears;       // all frames' clears; a frame holds its range

@@ -471,6 +471,8 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     // deferred-colour passes run every tile per record (their fragments are cheap: tests only)
     uint32_t *tile_area = (c.ctas && (c.order || c.classify) && !t.defer) ? tile_count + ntiles + 1 : nullptr;
     if ((rc = sc.take(S_TILE_START, (size_t)ntiles + 1, &tile_start))) return rc;
+    uint32_t *tile_frame = nullptr;  // batches: each tile's frame, found once by the range pass
+    if (t.nframes > 1 && (rc = sc.take(S_TILE_FRAME, ntiles, &tile_frame))) return rc;
     if (c.ctas && c.order && (rc = sc.take(S_ORDER, ntiles, &order))) return rc;
     if (c.ctas && (rc = sc.take(S_ORDER_AUX, kOrderAuxWords, &order_aux))) return rc;
     uint32_t scan_n = std::max<uint32_t>(std::max(tris, ntiles), 1);
@@ -560,6 +562,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ba.tile_count = tile_count;
     ba.tile_area = tile_area;
     ba.tile_start = tile_start;
+    ba.tile_frame = tile_frame;
     ba.total_dev = x.d_totals + 1;
     ba.sort_total_dev = x.d_totals + 3;
     ba.debug = x.d_totals + kDebugStatusWord;
@@ -608,6 +611,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ta.entries_cap = rec_cap ? pair_cap : 0u;
     ta.tile_start = tile_start;
     ta.tile_count = tile_count;
+    ta.tile_frame = rec_cap ? tile_frame : nullptr;  // written by the range pass, which runs with records
     ta.rasters = ga.rasters;
     ta.nrasters = std::max<uint32_t>(1, t.nrasters);
     ta.clears = reinterpret_cast<const ClearOp *>(ds + t.off_clears);

@@ -301,11 +301,23 @@ __global__ void __launch_bounds__(256) k_tile_bounds(BinArgs A)
     }
 }
 
-// end position - start = count; a tile without pairs has both still zero
+// end position - start = count; a tile without pairs has both still zero. Also the frame
+// that owns each tile (the last frame whose first tile is at or before it), so the tile
+// kernel reads it instead of searching the frame table per tile.
 __global__ void __launch_bounds__(256) k_tile_counts(BinArgs A)
 {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < A.ntiles; t += gridDim.x * blockDim.x)
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < A.ntiles; t += gridDim.x * blockDim.x) {
         A.tile_count[t] -= A.tile_start[t];
+        if (A.tile_frame) {
+            uint32_t lo = 0, hi = A.nframes - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (A.frames[mid].tile_base <= t) lo = mid;
+                else hi = mid - 1;
+            }
+            A.tile_frame[t] = lo;
+        }
+    }
 }
 
 int launch_tile_ranges(const BinArgs &a, cudaStream_t s)

@@ -470,7 +470,9 @@ __global__ void __launch_bounds__(TS *TS, tile_min_blocks<TS, EYE>()) k_tile(Til
                 if (A.tile_area && tile_class(A.tile_count, A.tile_area, tile, A.tile_shift) != (ROUNDS ? 0u : 1u))
                     tile = kSkipTile;
                 // the frame owning the tile: last frame whose tile_base <= tile
-                if (tile != kSkipTile && A.nframes > 1) {
+                if (tile != kSkipTile && A.nframes > 1 && A.tile_frame) {
+                    f = A.tile_frame[tile];
+                } else if (tile != kSkipTile && A.nframes > 1) {
                     uint32_t flo = 0, fhi = A.nframes - 1;
                     while (flo < fhi) {
                         const uint32_t mid = (flo + fhi + 1) >> 1;

@@ -22,7 +22,7 @@ struct GeomArgs {
     int32_t ndraws;
     const mtgl_vertex_state *vstates;
     const DevRaster *rasters;
-    PostVertex *verts;
+    PostVertices verts;
     PostEye *eyes;                    // null when no draw of the pass lights per fragment
     uint32_t total_slots;
     uint32_t total_tris;
@@ -38,6 +38,8 @@ struct GeomArgs {
     uint32_t *clip_sorted;            // the entries grouped by class (null: process clip_list as is)
     uint32_t *class_count;            // kClipBuckets counters (zeroed by the count launch)
     uint32_t *clip_count;             // their number (device; zeroed by the count launch)
+    uint32_t *emit_list;              // primitives the set-up emit pass writes (count pass output; unordered)
+    uint32_t *emit_count;             // their number (device; zeroed by the count launch)
     int32_t sms;
     uint32_t *debug;                  // status word of the debug bounds checks
 };

@@ -451,20 +451,20 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     PipeOut o;
 
     // scratch known before any count: vertices, triangle counts, tiles
-    PostVertex *verts = nullptr;
+    float4 *verts = nullptr;  // the three vertex streams, one after another
     PostEye *eyes = nullptr;
     uint32_t *tri_counts = nullptr, *tri_offsets = nullptr, *tile_count = nullptr, *tile_start = nullptr;
     uint32_t *scan_temp = nullptr, *order = nullptr, *order_aux = nullptr;
     float *records = nullptr, *eye_records = nullptr;
     uint32_t *rec_tiles = nullptr, *keys = nullptr, *vals = nullptr, *keys_alt = nullptr, *vals_alt = nullptr;
     uint32_t *radix_hist = nullptr;
-    if ((rc = sc.take(S_VERTS, slots, &verts))) return rc;
+    if ((rc = sc.take(S_VERTS, 3 * (size_t)slots, &verts))) return rc;
     if (eye && (rc = sc.take(S_EYES, slots, &eyes))) return rc;
     if ((rc = sc.take(S_TRI_COUNTS, tris, &tri_counts))) return rc;
     if ((rc = sc.take(S_TRI_OFFSETS, tris, &tri_offsets))) return rc;
     // clip list, its class words, the class-sorted list and the class counters
     uint32_t *clip_list = nullptr;
-    if ((rc = sc.take(S_CLIP_LIST, 3 * (size_t)tris + kClipBuckets, &clip_list))) return rc;
+    if ((rc = sc.take(S_CLIP_LIST, 4 * (size_t)tris + kClipBuckets, &clip_list))) return rc;
     // tile counts, then (persistent ordered launches) the per-tile record-box coverage
     if ((rc = sc.take(S_TILE_COUNT, 2 * ((size_t)ntiles + 1), &tile_count))) return rc;
     // record-box coverage per tile, for the split between tiles run by rounds and per record;
@@ -505,7 +505,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ga.rasters = reinterpret_cast<const DevRaster *>(ds + t.off_rs);
     ga.frames = reinterpret_cast<const DevFrame *>(ds + t.off_frames);
     ga.nframes = t.nframes;
-    ga.verts = verts;
+    ga.verts = PostVertices{verts, verts + slots, verts + 2 * (size_t)slots};
     ga.eyes = eyes;
     ga.total_slots = slots;
     ga.total_tris = tris;
@@ -518,6 +518,8 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     ga.clip_sorted = tris < (1u << 24) ? clip_list + 2 * (size_t)tris : nullptr;
     ga.class_count = clip_list + 3 * (size_t)tris;
     ga.clip_count = x.d_totals + 4;
+    ga.emit_list = clip_list + 3 * (size_t)tris + kClipBuckets;
+    ga.emit_count = x.d_totals + 5;
     ga.debug = x.d_totals + kDebugStatusWord;
     ga.sms = x.sms;
     int launches = 0;

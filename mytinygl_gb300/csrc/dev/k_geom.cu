@@ -166,14 +166,10 @@ __global__ void __launch_bounds__(128) k_vertex(GeomArgs A)
     if (t4.w != 0.0f && t4.w != 1.0f) uv = make_float2(t4.x / t4.w, t4.y / t4.w);
     else uv = make_float2(t4.x, t4.y);
 
-    PostVertex o;
-    o.clip = clip;
-    o.color = vc;
-    o.uv = uv;
-    o.eye_z = -eye.z;
-    o.pad = 0.0f;
     if (!debug_check(A.debug, g < A.total_slots, DBG_VERTEX_SLOT)) return;
-    A.verts[g] = o;
+    A.verts.clip[g] = clip;
+    A.verts.color[g] = vc;
+    A.verts.uvz[g] = make_float4(uv.x, uv.y, -eye.z, 0.0f);
     if (A.eyes) {
         PostEye e;
         e.pos_nx = make_float4(ep.x, ep.y, ep.z, en.x);
@@ -476,11 +472,11 @@ __device__ __forceinline__ uint32_t element_slot(const DevDraw &D, uint32_t e)
 template <bool EYE>
 __device__ __forceinline__ void load_cv(const GeomArgs &A, uint32_t slot, CVx<EYE> &v)
 {
-    const PostVertex pv = A.verts[slot];
-    v.clip = pv.clip;
-    v.col = pv.color;
-    v.uv = pv.uv;
-    v.ez = pv.eye_z;
+    v.clip = A.verts.clip[slot];
+    v.col = A.verts.color[slot];
+    const float4 uvz = A.verts.uvz[slot];
+    v.uv = make_float2(uvz.x, uvz.y);
+    v.ez = uvz.z;
     if constexpr (EYE) {
         const PostEye e = A.eyes[slot];
         v.ep = make_float3(e.pos_nx.x, e.pos_nx.y, e.pos_nx.z);
@@ -978,9 +974,15 @@ template <bool EMIT, bool EYE>
 __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
 {
     using V = CVx<EYE>;
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.total_tris) return;
-    if (EMIT && A.tri_counts[t] == 0) return;  // the count pass found nothing to emit
+    // the emit pass takes the primitives the count pass listed (those with records to write,
+    // straddling triangles aside); records go to each one's scanned offset, in order
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (EMIT) {
+        if (t >= min(*A.emit_count, A.total_tris)) return;
+        t = A.emit_list[t];
+    } else if (t >= A.total_tris) {
+        return;
+    }
     const Prim<EYE> P = prim_of<EYE>(A, t);
     const DevDraw &D = *P.D;
     const DevRaster &R = *P.R;
@@ -1021,9 +1023,20 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
         }
     }
     if (EMIT) return;
-    // Straddling triangles go to the clip list (k_clip stores their counts). The appends are
-    // combined per warp: one atomic for the list, one per class present in the warp.
+    // Primitives with records to write go to the emit list, straddling triangles to the clip
+    // list (k_clip stores their counts). The appends are combined per warp: one atomic per
+    // list, one per clip class present in the warp.
     const uint32_t active = __activemask();
+    const uint32_t emits = __ballot_sync(active, !straddles && produced != 0);
+    if (emits) {
+        const int lane = (int)(threadIdx.x & 31u);
+        const int first = __ffs(emits) - 1;
+        uint32_t base = 0;
+        if (lane == first) base = atomicAdd(A.emit_count, (uint32_t)__popc(emits));
+        base = __shfl_sync(active, base, first);
+        const uint32_t slot = base + (uint32_t)__popc(emits & ((1u << lane) - 1u));
+        if (!straddles && produced != 0 && slot < A.total_tris) A.emit_list[slot] = t;
+    }
     const uint32_t want = __ballot_sync(active, straddles);
     if (want) {
         const int lane = (int)(threadIdx.x & 31u);
@@ -1179,6 +1192,7 @@ int launch_setup_count(const GeomArgs &a, cudaStream_t s)
 {
     if (!a.total_tris) return 0;
     cudaMemsetAsync(a.clip_count, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(a.emit_count, 0, sizeof(uint32_t), s);
     if (a.clip_sorted) cudaMemsetAsync(a.class_count, 0, kClipBuckets * sizeof(uint32_t), s);
     return launch_setup<false>(a, s);
 }

@@ -116,13 +116,13 @@ __device__ __forceinline__ float depth_plane_bound(const float4 &zp, int minx, i
     return (z + 1.0f) * 0.5f;
 }
 
-// Post-transform vertex (vertex_t, graphics.h:438-446, without the unused object normal).
-struct __align__(16) PostVertex {
-    float4 clip;
-    float4 color;
-    float2 uv;
-    float eye_z;
-    float pad;
+// Post-transform vertices (vertex_t, graphics.h:438-446, without the unused object normal)
+// are stored as three streams of 16-byte words, one word per vertex slot each: the clip
+// position, the colour, and (u, v, eye z, 0). The count pass of set-up reads only the first.
+struct PostVertices {
+    float4 *clip;
+    float4 *color;
+    float4 *uvz;
 };
 struct __align__(16) PostEye {
     float4 pos_nx;   // eye_pos.xyz, eye_normal.x

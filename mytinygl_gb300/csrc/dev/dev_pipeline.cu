@@ -526,7 +526,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     launches += launch_vertex(ga, s);
     x.prof_mark();
     launches += launch_setup_count(ga, s);
-    launches += launch_scan(tri_counts, tri_offsets, tris, scan_temp, x.d_totals + 0, s);
+    launches += launch_scan(tri_counts, tri_offsets, tris, scan_temp, x.d_totals + 0, x.d_totals + kDebugStatusWord, s);
     CK(cudaGetLastError());
 
     uint32_t rec_cap = c.rec_cap;
@@ -573,7 +573,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     uint32_t pair_cap = c.pair_cap;
     if (rec_cap) {
         launches += launch_bin_count(ba, s);
-        launches += launch_scan(rec_tiles, rec_tiles, rec_cap, scan_temp, x.d_totals + 1, s);
+        launches += launch_scan(rec_tiles, rec_tiles, rec_cap, scan_temp, x.d_totals + 1, x.d_totals + kDebugStatusWord, s);
         CK(cudaGetLastError());
         if (c.exact) {
             CK(cudaMemcpyAsync(x.h_totals + 1, x.d_totals + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));

@@ -51,10 +51,30 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total)
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_block(const uint32_t *in, uint32_t *out, uint32_t n,
-                                                            uint32_t *block_sums, uint32_t *total_dev)
+// Single-pass exclusive scan with decoupled look-back (Merrill and Garland, "Single-pass
+// Parallel Prefix Scan with Decoupled Look-back", 2016). Blocks take their tile of kScanTile
+// values in the order they start (a ticket), publish the tile's sum, then walk back over
+// the tiles before theirs, adding published sums until one publishes its inclusive prefix.
+// A tile's status word: (flag << 32) | value, flag 0 = nothing yet, 1 = the tile's sum,
+// 2 = the inclusive prefix through the tile; written whole, so a reader sees one or the other.
+// A tile before a block's own was taken by a block that started earlier and publishes its sum
+// without waiting, so every wait ends; each is still bounded (kScanWaitLimit reads) and a
+// wait that runs out is recorded in the debug status word and counts the tile as empty.
+constexpr uint32_t kScanWaitLimit = 1u << 24;
+constexpr uint64_t kScanSum = 1ull << 32, kScanPrefix = 2ull << 32;
+
+__device__ __forceinline__ uint64_t ld_status(const uint64_t *p) { return *(const volatile uint64_t *)p; }
+__device__ __forceinline__ void st_status(uint64_t *p, uint64_t v) { *(volatile uint64_t *)p = v; }
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t *in, uint32_t *out, uint32_t n,
+                                                      uint64_t *status, uint32_t *ticket, uint32_t *total_dev,
+                                                      uint32_t *debug)
 {
-    const uint32_t base = blockIdx.x * (uint32_t)kScanTile + threadIdx.x * kScanItems;
+    __shared__ uint32_t s_tile, s_prefix;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * (uint32_t)kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     uint32_t sum = 0;
 #pragma unroll
@@ -62,54 +82,60 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_block(const uint32_t *in,
         v[i] = (base + i < n) ? in[base + i] : 0u;
         sum += v[i];
     }
-    uint32_t total;
-    uint32_t run = block_excl_scan(sum, &total);
+    uint32_t agg;
+    uint32_t run = block_excl_scan(sum, &agg);
+    if (threadIdx.x == 0) {
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            st_status(status, kScanPrefix | agg);
+        } else {
+            st_status(status + tile, kScanSum | agg);
+            for (uint32_t p = tile; p-- > 0;) {
+                uint64_t st = ld_status(status + p);
+                for (uint32_t w = 0; (st >> 32) == 0; w++) {
+                    if (w >= kScanWaitLimit) {
+                        if (debug) atomicCAS(debug, 0u, (uint32_t)DBG_SCAN_WAIT);
+                        break;
+                    }
+                    st = ld_status(status + p);
+                }
+                prefix += (uint32_t)st;
+                if ((st >> 32) == 2) break;
+            }
+            st_status(status + tile, kScanPrefix | (prefix + agg));
+        }
+        s_prefix = prefix;
+        if (tile + 1 == gridDim.x) *total_dev = prefix + agg;
+    }
+    __syncthreads();
+    run += s_prefix;
 #pragma unroll
     for (int i = 0; i < kScanItems; i++) {
         if (base + i < n) out[base + i] = run;
         run += v[i];
     }
-    if (threadIdx.x == 0) {
-        if (block_sums) block_sums[blockIdx.x] = total;
-        if (total_dev) *total_dev = total;
-    }
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t *out, uint32_t n, const uint32_t *block_offsets)
-{
-    const uint32_t add = block_offsets[blockIdx.x];
-    const uint32_t base = blockIdx.x * (uint32_t)kScanTile + threadIdx.x * kScanItems;
-#pragma unroll
-    for (int i = 0; i < kScanItems; i++)
-        if (base + i < n) out[base + i] += add;
 }
 
 size_t scan_temp_words(uint32_t n)
 {
-    size_t words = 0;
-    while (n > (uint32_t)kScanTile) {
-        n = (n + kScanTile - 1) / kScanTile;
-        words += ((size_t)n + 63) & ~(size_t)63;
-    }
-    return words + 64;
+    // a 64-bit status word per tile, then the ticket
+    return 2 * (((size_t)n + kScanTile - 1) / kScanTile) + 64;
 }
 
-int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, uint32_t *total_dev, cudaStream_t s)
+int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, uint32_t *total_dev, uint32_t *debug,
+                cudaStream_t s)
 {
     if (n == 0) {
         cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), s);
         return 0;
     }
     const uint32_t nb = (n + kScanTile - 1) / kScanTile;
-    if (nb == 1) {
-        k_scan_block<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr, total_dev);
-        return 1;
-    }
-    k_scan_block<<<nb, kScanThreads, 0, s>>>(in, out, n, temp, nullptr);
-    uint32_t *next = temp + (((size_t)nb + 63) & ~(size_t)63);
-    int k = launch_scan(temp, temp, nb, next, total_dev, s);
-    k_scan_add<<<nb, kScanThreads, 0, s>>>(out, n, temp);
-    return k + 2;
+    // temp is 8-byte aligned (scratch slices start on 256-byte boundaries)
+    uint64_t *status = reinterpret_cast<uint64_t *>(temp);
+    uint32_t *ticket = temp + 2 * (size_t)nb;
+    cudaMemsetAsync(temp, 0, (2 * (size_t)nb + 1) * sizeof(uint32_t), s);
+    k_scan<<<nb, kScanThreads, 0, s>>>(in, out, n, status, ticket, total_dev, debug);
+    return 1;
 }
 
 // ------------------------------------------------------------------ record -> tiles
@@ -561,7 +587,8 @@ int launch_bin_sort(BinArgs &a, cudaStream_t s)
         const int nbits = (bits - shift) < width ? (bits - shift) : width;
         const uint32_t mask = (1u << nbits) - 1u;
         k_radix_hist<<<nb, kRadixThreads, 0, s>>>(a.keys, n, a.total_dev, shift, mask, a.radix_hist, nb);
-        launches += 2 + launch_scan(a.radix_hist, a.radix_hist, nb * (mask + 1u), a.scan_temp, a.sort_total_dev, s);
+        launches += 2 + launch_scan(a.radix_hist, a.radix_hist, nb * (mask + 1u), a.scan_temp, a.sort_total_dev,
+                                    a.debug, s);
         k_radix_scatter<<<nb, kRadixThreads, 0, s>>>(a.keys, a.vals, n, a.total_dev, shift, mask, a.radix_hist, nb,
                                                      a.keys_alt, a.vals_alt);
         uint32_t *tk = a.keys, *tv = a.vals;

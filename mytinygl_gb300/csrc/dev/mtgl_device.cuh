@@ -30,6 +30,9 @@ enum DebugSite : uint32_t {
     DBG_BIN_TILE = 4,      // binning: tile id of a sorted pair
     DBG_VERTEX_SLOT = 5,   // K1: vertex slot
     DBG_SETUP_RECORD = 6,  // K2: record position
+    // Not an index check, and recorded by every build: a scan's bounded wait for an earlier
+    // tile's sum ran out (never expected; the pass's results are then wrong).
+    DBG_SCAN_WAIT = 7,
 };
 __device__ __forceinline__ bool debug_check(uint32_t *status, bool ok, uint32_t site)
 {

@@ -54,7 +54,8 @@ int launch_setup_emit(const GeomArgs &a, cudaStream_t s);
 // Every launcher returns the number of kernels it launched.
 
 // Device-wide exclusive scan of n uint32 values (in place allowed; one launch); writes the
-// total to *total_dev. temp must hold scan_temp_words(n) words, 8-byte aligned; debug is the
+// total to *total_dev. in and out 16-byte aligned; temp must hold scan_temp_words(n) words,
+// 8-byte aligned; debug is the
 // status word its bounded waits report to (may be null).
 size_t scan_temp_words(uint32_t n);
 int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, uint32_t *total_dev, uint32_t *debug,

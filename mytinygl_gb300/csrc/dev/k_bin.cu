@@ -54,7 +54,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total)
 // Single-pass exclusive scan with decoupled look-back (Merrill and Garland, "Single-pass
 // Parallel Prefix Scan with Decoupled Look-back", 2016). Blocks take their tile of kScanTile
 // values in the order they start (a ticket), publish the tile's sum, then walk back over
-// the tiles before theirs, adding published sums until one publishes its inclusive prefix.
+// the tiles before theirs, 32 at a time, adding published sums until one publishes its
+// inclusive prefix.
 // A tile's status word: (flag << 32) | value, flag 0 = nothing yet, 1 = the tile's sum,
 // 2 = the inclusive prefix through the tile; written whole, so a reader sees one or the other.
 // A tile before a block's own was taken by a block that started earlier and publishes its sum
@@ -75,44 +76,67 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t *in, uint3
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t base = tile * (uint32_t)kScanTile + threadIdx.x * kScanItems;
+    // each thread's 8 values as two 16-byte words (base is a multiple of 8 words)
     uint32_t v[kScanItems];
+    if (base + kScanItems <= n) {
+        const uint4 a = *reinterpret_cast<const uint4 *>(in + base), b = *reinterpret_cast<const uint4 *>(in + base + 4);
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; i++) v[i] = (base + i < n) ? in[base + i] : 0u;
+    }
     uint32_t sum = 0;
 #pragma unroll
-    for (int i = 0; i < kScanItems; i++) {
-        v[i] = (base + i < n) ? in[base + i] : 0u;
-        sum += v[i];
-    }
+    for (int i = 0; i < kScanItems; i++) sum += v[i];
     uint32_t agg;
     uint32_t run = block_excl_scan(sum, &agg);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
+        // warp 0 looks back 32 tiles at a time: lane k reads the status of tile (window - k)
+        const uint32_t lane = threadIdx.x;
         uint32_t prefix = 0;
         if (tile == 0) {
-            st_status(status, kScanPrefix | agg);
+            if (lane == 0) st_status(status, kScanPrefix | agg);
         } else {
-            st_status(status + tile, kScanSum | agg);
-            for (uint32_t p = tile; p-- > 0;) {
-                uint64_t st = ld_status(status + p);
-                for (uint32_t w = 0; (st >> 32) == 0; w++) {
-                    if (w >= kScanWaitLimit) {
+            if (lane == 0) st_status(status + tile, kScanSum | agg);
+            for (int64_t win = (int64_t)tile - 1;; win -= 32) {
+                const int64_t p = win - (int64_t)lane;
+                uint64_t st = p >= 0 ? ld_status(status + p) : kScanPrefix;  // before tile 0: a zero prefix
+                for (uint32_t w = 0; !__all_sync(0xffffffffu, (st >> 32) != 0);) {
+                    if (++w < kScanWaitLimit) {
+                        if ((st >> 32) == 0) st = ld_status(status + p);
+                    } else if ((st >> 32) == 0) {
+                        st = kScanSum;  // counted as empty
                         if (debug) atomicCAS(debug, 0u, (uint32_t)DBG_SCAN_WAIT);
-                        break;
                     }
-                    st = ld_status(status + p);
                 }
-                prefix += (uint32_t)st;
-                if ((st >> 32) == 2) break;
+                // the nearest tile with its inclusive prefix ends the walk; the nearer ones add sums
+                const uint32_t prefixed = __ballot_sync(0xffffffffu, (st >> 32) == 2);
+                const uint32_t upto = prefixed ? (uint32_t)__ffs(prefixed) - 1u : 31u;
+                prefix += __reduce_add_sync(0xffffffffu, lane <= upto ? (uint32_t)st : 0u);
+                if (prefixed) break;
             }
-            st_status(status + tile, kScanPrefix | (prefix + agg));
+            if (lane == 0) st_status(status + tile, kScanPrefix | (prefix + agg));
         }
-        s_prefix = prefix;
-        if (tile + 1 == gridDim.x) *total_dev = prefix + agg;
+        if (lane == 0) {
+            s_prefix = prefix;
+            if (tile + 1 == gridDim.x) *total_dev = prefix + agg;
+        }
     }
     __syncthreads();
     run += s_prefix;
+    uint32_t o[kScanItems];
 #pragma unroll
     for (int i = 0; i < kScanItems; i++) {
-        if (base + i < n) out[base + i] = run;
+        o[i] = run;
         run += v[i];
+    }
+    if (base + kScanItems <= n) {
+        *reinterpret_cast<uint4 *>(out + base) = make_uint4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<uint4 *>(out + base + 4) = make_uint4(o[4], o[5], o[6], o[7]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; i++)
+            if (base + i < n) out[base + i] = o[i];
     }
 }
 

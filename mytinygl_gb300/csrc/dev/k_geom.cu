@@ -977,86 +977,97 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
     // the emit pass takes the primitives the count pass listed (those with records to write,
     // straddling triangles aside); records go to each one's scanned offset, in order
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = true;
     if (EMIT) {
         if (t >= min(*A.emit_count, A.total_tris)) return;
         t = A.emit_list[t];
-    } else if (t >= A.total_tris) {
-        return;
+    } else {
+        live = t < A.total_tris;  // the count pass keeps every thread for its block's appends
     }
-    const Prim<EYE> P = prim_of<EYE>(A, t);
-    const DevDraw &D = *P.D;
-    const DevRaster &R = *P.R;
-    const RecOut o = rec_out(A, t, EMIT, EYE);
     uint32_t produced = 0;
     bool straddles = false;  // count pass: goes to the clip list, with its clip class
     uint32_t cls = 0;
 
-    if (D.mode == GL_POINTS) {
-        V v;
-        load_cv(A, element_slot(D, P.k), v);
-        produced = vertex_point(R, D.raster, P.frame, P.dims, v, o.rec(0));
-    } else if (D.mode == GL_LINES || D.mode == GL_LINE_STRIP || D.mode == GL_LINE_LOOP) {
-        uint32_t e0, e1;
-        element_pair(D.mode, P.k, (uint32_t)D.count, e0, e1);
-        V v0, v1;
-        load_cv(A, element_slot(D, e0), v0);
-        load_cv(A, element_slot(D, e1), v1);
-        produced = segment_line(R, D.raster, P.frame, P.dims, v0, v1, o.rec(0));
-    } else {
-        uint32_t e0, e1, e2;
-        element_triple(D.mode, P.k, e0, e1, e2);
-        V v0, v1, v2;
-        load_cv(A, element_slot(D, e0), v0);
-        load_cv(A, element_slot(D, e1), v1);
-        load_cv(A, element_slot(D, e2), v2);
-        const uint32_t m0 = inside_mask(v0.clip), m1 = inside_mask(v1.clip), m2 = inside_mask(v2.clip);
-        const int start = clip_start(m0, m1, m2);
-        if (start == kClipNone) {  // the clipper would return the triangle unchanged
-            persp_divide(v0);
-            persp_divide(v1);
-            persp_divide(v2);
-            produced = setup_fan_tri(R, D.raster, P.frame, P.dims, v0, v1, v2, o, 0);
-        } else if (start != kClipEmpty) {
-            if (EMIT) return;  // k_clip emits it
-            cls = A.clip_sorted ? clip_class(m0, m1, m2, start) : 0u;
-            straddles = true;
+    if (live) {
+        const Prim<EYE> P = prim_of<EYE>(A, t);
+        const DevDraw &D = *P.D;
+        const DevRaster &R = *P.R;
+        const RecOut o = rec_out(A, t, EMIT, EYE);
+        if (D.mode == GL_POINTS) {
+            V v;
+            load_cv(A, element_slot(D, P.k), v);
+            produced = vertex_point(R, D.raster, P.frame, P.dims, v, o.rec(0));
+        } else if (D.mode == GL_LINES || D.mode == GL_LINE_STRIP || D.mode == GL_LINE_LOOP) {
+            uint32_t e0, e1;
+            element_pair(D.mode, P.k, (uint32_t)D.count, e0, e1);
+            V v0, v1;
+            load_cv(A, element_slot(D, e0), v0);
+            load_cv(A, element_slot(D, e1), v1);
+            produced = segment_line(R, D.raster, P.frame, P.dims, v0, v1, o.rec(0));
+        } else {
+            uint32_t e0, e1, e2;
+            element_triple(D.mode, P.k, e0, e1, e2);
+            V v0, v1, v2;
+            load_cv(A, element_slot(D, e0), v0);
+            load_cv(A, element_slot(D, e1), v1);
+            load_cv(A, element_slot(D, e2), v2);
+            const uint32_t m0 = inside_mask(v0.clip), m1 = inside_mask(v1.clip), m2 = inside_mask(v2.clip);
+            const int start = clip_start(m0, m1, m2);
+            if (start == kClipNone) {  // the clipper would return the triangle unchanged
+                persp_divide(v0);
+                persp_divide(v1);
+                persp_divide(v2);
+                produced = setup_fan_tri(R, D.raster, P.frame, P.dims, v0, v1, v2, o, 0);
+            } else if (start != kClipEmpty) {
+                if (EMIT) return;  // k_clip emits it
+                cls = A.clip_sorted ? clip_class(m0, m1, m2, start) : 0u;
+                straddles = true;
+            }
         }
     }
     if (EMIT) return;
     // Primitives with records to write go to the emit list, straddling triangles to the clip
-    // list (k_clip stores their counts). The appends are combined per warp: one atomic per
-    // list, one per clip class present in the warp.
-    const uint32_t active = __activemask();
-    const uint32_t emits = __ballot_sync(active, !straddles && produced != 0);
-    if (emits) {
-        const int lane = (int)(threadIdx.x & 31u);
-        const int first = __ffs(emits) - 1;
-        uint32_t base = 0;
-        if (lane == first) base = atomicAdd(A.emit_count, (uint32_t)__popc(emits));
-        base = __shfl_sync(active, base, first);
-        const uint32_t slot = base + (uint32_t)__popc(emits & ((1u << lane) - 1u));
-        if (!straddles && produced != 0 && slot < A.total_tris) A.emit_list[slot] = t;
+    // list (k_clip stores their counts). The appends are combined per block: one atomic per
+    // list and block, and per warp one per clip class present in the warp.
+    constexpr int kWarps = 128 / 32;
+    __shared__ uint32_t s_n[2][kWarps], s_at[2][kWarps];  // per list and warp: entries, first slot
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t below = (1u << lane) - 1u;
+    const bool emit = live && !straddles && produced != 0;
+    const uint32_t emits = __ballot_sync(0xffffffffu, emit), want = __ballot_sync(0xffffffffu, straddles);
+    if (lane == 0) {
+        s_n[0][warp] = (uint32_t)__popc(emits);
+        s_n[1][warp] = (uint32_t)__popc(want);
     }
-    const uint32_t want = __ballot_sync(active, straddles);
+    __syncthreads();
+    if (threadIdx.x < 2) {  // thread 0: the emit list, thread 1: the clip list
+        const uint32_t l = threadIdx.x;
+        uint32_t total = 0;
+        for (int w = 0; w < kWarps; w++) total += s_n[l][w];
+        uint32_t at = total ? atomicAdd(l == 0 ? A.emit_count : A.clip_count, total) : 0u;
+        for (int w = 0; w < kWarps; w++) {
+            s_at[l][w] = at;
+            at += s_n[l][w];
+        }
+    }
+    __syncthreads();
+    if (emit) {
+        const uint32_t slot = s_at[0][warp] + (uint32_t)__popc(emits & below);
+        if (slot < A.total_tris) A.emit_list[slot] = t;
+    }
     if (want) {
-        const int lane = (int)(threadIdx.x & 31u);
-        const uint32_t below = (1u << lane) - 1u;
-        const int first = __ffs(want) - 1;
-        uint32_t base = 0;
-        if (lane == first) base = atomicAdd(A.clip_count, (uint32_t)__popc(want));
-        base = __shfl_sync(active, base, first);
         uint32_t rank = 0;
         const uint32_t bucket = cls * kClipSlots + (blockIdx.x & (kClipSlots - 1));
         if (A.clip_sorted) {
-            const uint32_t peers = __match_any_sync(active, straddles ? bucket : 0xFFFFFFFFu);
+            const uint32_t peers = __match_any_sync(0xffffffffu, straddles ? bucket : 0xFFFFFFFFu);
             const int leader = __ffs(peers) - 1;
             uint32_t rb = 0;
-            if (straddles && lane == leader) rb = atomicAdd(A.class_count + bucket, (uint32_t)__popc(peers));
-            rb = __shfl_sync(active, rb, leader);
+            if (straddles && (int)lane == leader) rb = atomicAdd(A.class_count + bucket, (uint32_t)__popc(peers));
+            rb = __shfl_sync(0xffffffffu, rb, leader);
             rank = rb + (uint32_t)__popc(peers & below);
         }
         if (straddles) {
-            const uint32_t slot = base + (uint32_t)__popc(want & below);
+            const uint32_t slot = s_at[1][warp] + (uint32_t)__popc(want & below);
             if (slot < A.total_tris) {
                 A.clip_list[slot] = t;
                 if (A.clip_sorted) A.clip_class[slot] = (bucket << 20) | rank;
@@ -1064,7 +1075,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
             return;
         }
     }
-    A.tri_counts[t] = produced;
+    if (live) A.tri_counts[t] = produced;
 }
 
 // The listed triangles: Sutherland-Hodgman from the first plane that is not all-inside, then

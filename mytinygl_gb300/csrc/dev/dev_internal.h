@@ -137,7 +137,7 @@ struct Exec {
     uint8_t *dstage = nullptr;
     size_t dcap = 0;
     uint64_t allocs = 0;  // device allocations of the staging copy
-    uint32_t *d_totals = nullptr;  // [0] records, [1] pairs, [2] tiles' records, [3] sort scratch, [4] clip list, [5] emit list,
+    uint32_t *d_totals = nullptr;  // [0] records, [1] pairs, [2] tiles' records, [3] sort scratch, [4] clip list, [5] emit list (GeomArgs::list_counts),
                                    // [kDebugStatusWord] the debug bounds checks' status
     uint32_t *h_totals = nullptr;  // pinned copy of [0..1]
     unsigned long long *d_frags = nullptr;

@@ -37,9 +37,9 @@ struct GeomArgs {
     uint32_t *clip_class;             // per entry: bucket << 20 | rank within the bucket
     uint32_t *clip_sorted;            // the entries grouped by class (null: process clip_list as is)
     uint32_t *class_count;            // kClipBuckets counters (zeroed by the count launch)
-    uint32_t *clip_count;             // their number (device; zeroed by the count launch)
     uint32_t *emit_list;              // primitives the set-up emit pass writes (count pass output; unordered)
-    uint32_t *emit_count;             // their number (device; zeroed by the count launch)
+    uint32_t *list_counts;            // entries of [0] the clip list, [1] the emit list (device; zeroed
+                                      // by the count launch)
     int32_t sms;
     uint32_t *debug;                  // status word of the debug bounds checks
 };

@@ -517,9 +517,8 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     // are every kClipSlots-th of 128 triangles), so a rank fits the class word's 20 bits
     ga.clip_sorted = tris < (1u << 24) ? clip_list + 2 * (size_t)tris : nullptr;
     ga.class_count = clip_list + 3 * (size_t)tris;
-    ga.clip_count = x.d_totals + 4;
     ga.emit_list = clip_list + 3 * (size_t)tris + kClipBuckets;
-    ga.emit_count = x.d_totals + 5;
+    ga.list_counts = x.d_totals + 4;
     ga.debug = x.d_totals + kDebugStatusWord;
     ga.sms = x.sms;
     int launches = 0;

@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t *in, uint3
                                                       uint32_t *debug)
 {
     __shared__ uint32_t s_tile, s_prefix;
-    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    if (threadIdx.x == 0) s_tile = gridDim.x == 1 ? 0u : atomicAdd(ticket, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t base = tile * (uint32_t)kScanTile + threadIdx.x * kScanItems;
@@ -154,10 +154,11 @@ int launch_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *temp, u
         return 0;
     }
     const uint32_t nb = (n + kScanTile - 1) / kScanTile;
-    // temp is 8-byte aligned (scratch slices start on 256-byte boundaries)
+    // temp is 8-byte aligned (scratch slices start on 256-byte boundaries); a single tile needs
+    // neither tickets nor statuses (and so no clearing)
     uint64_t *status = reinterpret_cast<uint64_t *>(temp);
     uint32_t *ticket = temp + 2 * (size_t)nb;
-    cudaMemsetAsync(temp, 0, (2 * (size_t)nb + 1) * sizeof(uint32_t), s);
+    if (nb > 1) cudaMemsetAsync(temp, 0, (2 * (size_t)nb + 1) * sizeof(uint32_t), s);
     k_scan<<<nb, kScanThreads, 0, s>>>(in, out, n, status, ticket, total_dev, debug);
     return 1;
 }

@@ -979,7 +979,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = true;
     if (EMIT) {
-        if (t >= min(*A.emit_count, A.total_tris)) return;
+        if (t >= min(A.list_counts[1], A.total_tris)) return;
         t = A.emit_list[t];
     } else {
         live = t < A.total_tris;  // the count pass keeps every thread for its block's appends
@@ -1044,7 +1044,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
         const uint32_t l = threadIdx.x;
         uint32_t total = 0;
         for (int w = 0; w < kWarps; w++) total += s_n[l][w];
-        uint32_t at = total ? atomicAdd(l == 0 ? A.emit_count : A.clip_count, total) : 0u;
+        uint32_t at = total ? atomicAdd(A.list_counts + (l == 0 ? 1 : 0), total) : 0u;
         for (int w = 0; w < kWarps; w++) {
             s_at[l][w] = at;
             at += s_n[l][w];
@@ -1085,7 +1085,7 @@ template <bool EMIT, bool EYE>
 __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
 {
     using V = CVx<EYE>;
-    const uint32_t n = min(*A.clip_count, A.total_tris);
+    const uint32_t n = min(A.list_counts[0], A.total_tris);
     const uint32_t *list = A.clip_sorted ? A.clip_sorted : A.clip_list;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t t = list[i];
@@ -1128,7 +1128,7 @@ __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
 // (buckets class-major, so each class's entries are contiguous)
 __global__ void __launch_bounds__(256) k_clip_sort(GeomArgs A)
 {
-    const uint32_t n = min(*A.clip_count, A.total_tris);
+    const uint32_t n = min(A.list_counts[0], A.total_tris);
     if (blockIdx.x * blockDim.x >= n) return;  // no entries for this block (uniform)
     // exclusive prefix of the bucket counts (class-major), in shared memory: each thread sums
     // kPer consecutive buckets, the warps scan those sums, then each thread writes its starts
@@ -1202,8 +1202,7 @@ int launch_setup(const GeomArgs &a, cudaStream_t s)
 int launch_setup_count(const GeomArgs &a, cudaStream_t s)
 {
     if (!a.total_tris) return 0;
-    cudaMemsetAsync(a.clip_count, 0, sizeof(uint32_t), s);
-    cudaMemsetAsync(a.emit_count, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(a.list_counts, 0, 2 * sizeof(uint32_t), s);
     if (a.clip_sorted) cudaMemsetAsync(a.class_count, 0, kClipBuckets * sizeof(uint32_t), s);
     return launch_setup<false>(a, s);
 }

@@ -224,6 +224,17 @@ __device__ __forceinline__ CVx<EYE> cv_lerp(const CVx<EYE> &a, const CVx<EYE> &b
     return v;
 }
 
+// A vertex through clipping when only its position matters: the count pass of a filled
+// triangle's clip, where whether and how many records come out depends on positions alone.
+struct ClipPos {
+    float4 clip;
+};
+__device__ __forceinline__ ClipPos cv_lerp(const ClipPos &a, const ClipPos &b, float t)
+{
+    return ClipPos{make_float4(a.clip.x + t * (b.clip.x - a.clip.x), a.clip.y + t * (b.clip.y - a.clip.y),
+                               a.clip.z + t * (b.clip.z - a.clip.z), a.clip.w + t * (b.clip.w - a.clip.w))};
+}
+
 __device__ __forceinline__ float plane_dist(const float4 &v, int p)
 {
     switch (p) {
@@ -796,6 +807,63 @@ struct RecOut {
     }
 };
 
+// The part of a fan triangle's set-up that decides whether it produces a record: screen
+// positions, culling, and for a filled triangle the box clamped to the viewport, scissor and
+// framebuffer and the area test (rasterize_triangle_smooth's set-up, raster.c:451-529).
+// Returns kTriNone (no record), kTriPolygonMode (drawn as points or lines: the caller's
+// polygon-mode path; only the positions and `back` are set) or kTriFill (a record).
+constexpr int kTriNone = 0, kTriPolygonMode = 1, kTriFill = 2;
+struct TriBox {
+    int32_t x[3], y[3];
+    int32_t minX, minY, maxX, maxY;
+    float area;
+    bool back;
+};
+__device__ __forceinline__ int tri_box(const mtgl_raster_state &rs, const FrameDims &dims, const float4 &a,
+                                       const float4 &b, const float4 &c, TriBox &t)
+{
+    ndc_to_screen(rs, a.x, a.y, t.x[0], t.y[0]);
+    ndc_to_screen(rs, b.x, b.y, t.x[1], t.y[1]);
+    ndc_to_screen(rs, c.x, c.y, t.x[2], t.y[2]);
+    const int32_t x0 = t.x[0], y0 = t.y[0], x1 = t.x[1], y1 = t.y[1], x2 = t.x[2], y2 = t.y[2];
+    const float sa = idiff(x1, x0) * idiff(y2, y0) - idiff(x2, x0) * idiff(y1, y0);
+    if (culled(rs, sa)) return kTriNone;
+    t.back = (rs.front_face == GL_CCW) ? (sa >= 0) : (sa < 0);
+    const uint32_t pm = t.back ? rs.polygon_mode_back : rs.polygon_mode_front;
+    if (pm == GL_POINT || pm == GL_LINE) return kTriPolygonMode;
+
+    int32_t minX = x0 < x1 ? (x0 < x2 ? x0 : x2) : (x1 < x2 ? x1 : x2);
+    int32_t minY = y0 < y1 ? (y0 < y2 ? y0 : y2) : (y1 < y2 ? y1 : y2);
+    int32_t maxX = x0 > x1 ? (x0 > x2 ? x0 : x2) : (x1 > x2 ? x1 : x2);
+    int32_t maxY = y0 > y1 ? (y0 > y2 ? y0 : y2) : (y1 > y2 ? y1 : y2);
+    if (minX < rs.viewport[0]) minX = rs.viewport[0];
+    if (minY < rs.viewport[1]) minY = rs.viewport[1];
+    if (maxX >= rs.viewport[0] + rs.viewport[2]) maxX = rs.viewport[0] + rs.viewport[2] - 1;
+    if (maxY >= rs.viewport[1] + rs.viewport[3]) maxY = rs.viewport[1] + rs.viewport[3] - 1;
+    if (rs.scissor_test) {
+        if (minX < rs.scissor[0]) minX = rs.scissor[0];
+        if (minY < rs.scissor[1]) minY = rs.scissor[1];
+        if (maxX >= rs.scissor[0] + rs.scissor[2]) maxX = rs.scissor[0] + rs.scissor[2] - 1;
+        if (maxY >= rs.scissor[1] + rs.scissor[3]) maxY = rs.scissor[1] + rs.scissor[3] - 1;
+    }
+    if (minX > maxX || minY > maxY) return kTriNone;
+    // pixels outside the framebuffer read defaults and write nothing (framebuffer.h:92-134)
+    if (minX < 0) minX = 0;
+    if (minY < 0) minY = 0;
+    if (maxX > dims.width - 1) maxX = dims.width - 1;
+    if (maxY > dims.height - 1) maxY = dims.height - 1;
+    if (minX > maxX || minY > maxY) return kTriNone;
+
+    const float fx0 = (float)x0, fy0 = (float)y0, fx1 = (float)x1, fy1 = (float)y1, fx2 = (float)x2, fy2 = (float)y2;
+    t.area = (fx2 - fx0) * (fy1 - fy0) - (fy2 - fy0) * (fx1 - fx0);
+    if (fabsf(t.area) < 0.5f) return kTriNone;
+    t.minX = minX;
+    t.minY = minY;
+    t.maxX = maxX;
+    t.maxY = maxY;
+    return kTriFill;
+}
+
 // Per fan triangle: the setup half of rasterize_triangle_smooth. Returns true when the
 // triangle produces a record; writes it when `rec` is non-null.
 template <class V>
@@ -804,15 +872,13 @@ __device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t r
                                                   const RecOut &o, uint32_t at)
 {
     const mtgl_raster_state &rs = R.rs;
-    int32_t x0, y0, x1, y1, x2, y2;
-    ndc_to_screen(rs, a.clip.x, a.clip.y, x0, y0);
-    ndc_to_screen(rs, b.clip.x, b.clip.y, x1, y1);
-    ndc_to_screen(rs, c.clip.x, c.clip.y, x2, y2);
-    const float sa = idiff(x1, x0) * idiff(y2, y0) - idiff(x2, x0) * idiff(y1, y0);
-    if (culled(rs, sa)) return 0;
-    const bool back = (rs.front_face == GL_CCW) ? (sa >= 0) : (sa < 0);
-    const uint32_t pm = back ? rs.polygon_mode_back : rs.polygon_mode_front;
-    if (pm == GL_POINT || pm == GL_LINE) {
+    TriBox tb;
+    const int kind = tri_box(rs, dims, a.clip, b.clip, c.clip, tb);
+    if (kind == kTriNone) return 0;
+    const int32_t x0 = tb.x[0], y0 = tb.y[0], x1 = tb.x[1], y1 = tb.y[1], x2 = tb.x[2], y2 = tb.y[2];
+    const bool back = tb.back;
+    if (kind == kTriPolygonMode) {
+        const uint32_t pm = back ? rs.polygon_mode_back : rs.polygon_mode_front;
         // render_triangle's polygon modes (raster.c:901-958): vertex colours, lit per vertex
         // under GL_PHONG (phong_vertex_colors), then three points or three edges
         float4 c0 = a.col, c1 = b.col, c2 = c.col;
@@ -838,33 +904,10 @@ __device__ __forceinline__ uint32_t setup_fan_tri(const DevRaster &R, uint32_t r
     }
     float *rec = o.rec(at);
     float *eyerec = o.eye(at);
-
-    int32_t minX = x0 < x1 ? (x0 < x2 ? x0 : x2) : (x1 < x2 ? x1 : x2);
-    int32_t minY = y0 < y1 ? (y0 < y2 ? y0 : y2) : (y1 < y2 ? y1 : y2);
-    int32_t maxX = x0 > x1 ? (x0 > x2 ? x0 : x2) : (x1 > x2 ? x1 : x2);
-    int32_t maxY = y0 > y1 ? (y0 > y2 ? y0 : y2) : (y1 > y2 ? y1 : y2);
-    if (minX < rs.viewport[0]) minX = rs.viewport[0];
-    if (minY < rs.viewport[1]) minY = rs.viewport[1];
-    if (maxX >= rs.viewport[0] + rs.viewport[2]) maxX = rs.viewport[0] + rs.viewport[2] - 1;
-    if (maxY >= rs.viewport[1] + rs.viewport[3]) maxY = rs.viewport[1] + rs.viewport[3] - 1;
-    if (rs.scissor_test) {
-        if (minX < rs.scissor[0]) minX = rs.scissor[0];
-        if (minY < rs.scissor[1]) minY = rs.scissor[1];
-        if (maxX >= rs.scissor[0] + rs.scissor[2]) maxX = rs.scissor[0] + rs.scissor[2] - 1;
-        if (maxY >= rs.scissor[1] + rs.scissor[3]) maxY = rs.scissor[1] + rs.scissor[3] - 1;
-    }
-    if (minX > maxX || minY > maxY) return 0;
-    // pixels outside the framebuffer read defaults and write nothing (framebuffer.h:92-134)
-    if (minX < 0) minX = 0;
-    if (minY < 0) minY = 0;
-    if (maxX > dims.width - 1) maxX = dims.width - 1;
-    if (maxY > dims.height - 1) maxY = dims.height - 1;
-    if (minX > maxX || minY > maxY) return 0;
-
-    const float fx0 = (float)x0, fy0 = (float)y0, fx1 = (float)x1, fy1 = (float)y1, fx2 = (float)x2, fy2 = (float)y2;
-    const float area = (fx2 - fx0) * (fy1 - fy0) - (fy2 - fy0) * (fx1 - fx0);
-    if (fabsf(area) < 0.5f) return 0;
     if (!rec) return 1;
+    const int32_t minX = tb.minX, minY = tb.minY, maxX = tb.maxX, maxY = tb.maxY;
+    const float fx0 = (float)x0, fy0 = (float)y0, fx1 = (float)x1, fy1 = (float)y1, fx2 = (float)x2, fy2 = (float)y2;
+    const float area = tb.area;
 
     const float inv_area = 1.0f / area;
     float lod = 0.0f;
@@ -1078,6 +1121,66 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
     if (live) A.tri_counts[t] = produced;
 }
 
+// A straddling triangle clipped (from its first crossed plane: in registers when that plane is
+// the only one crossed, else the general clipper), divided and fanned; returns the records
+// produced, written through `o` in the emit pass.
+template <class V>
+__device__ __forceinline__ uint32_t clip_fan(const DevRaster &R, uint32_t raster_id, uint32_t frame,
+                                             const FrameDims &dims, const V &v0, const V &v1, const V &v2,
+                                             const RecOut &o)
+{
+    const int start = clip_start(inside_mask(v0.clip), inside_mask(v1.clip), inside_mask(v2.clip));
+    uint32_t produced = 0;
+    V bufA[kClipMax];
+    int nv = 0;
+    if (start < kClipNone) {
+        nv = clip_one_plane(v0, v1, v2, start, bufA[0], bufA[1], bufA[2], bufA[3]);
+        if (!nv) {
+            V bufB[kClipMax];
+            bufA[0] = v0;
+            bufA[1] = v1;
+            bufA[2] = v2;
+            nv = clip_triangle(bufA, bufB, start);
+        }
+    }
+    if (nv >= 3) {
+        for (int j = 0; j < nv; j++) persp_divide(bufA[j]);
+        for (int j = 1; j + 1 < nv; j++)
+            produced += setup_fan_tri(R, raster_id, frame, dims, bufA[0], bufA[j], bufA[j + 1], o, produced);
+    }
+    return produced;
+}
+
+// clip_fan's count for a filled triangle (both polygon modes GL_FILL): the same clipping of
+// the positions (the other attributes never decide a filled triangle's records), then
+// tri_box per fan triangle.
+__device__ __forceinline__ uint32_t clip_fan_count(const DevRaster &R, const FrameDims &dims, const ClipPos &v0,
+                                                   const ClipPos &v1, const ClipPos &v2)
+{
+    const int start = clip_start(inside_mask(v0.clip), inside_mask(v1.clip), inside_mask(v2.clip));
+    ClipPos bufA[kClipMax];
+    int nv = 0;
+    if (start < kClipNone) {
+        nv = clip_one_plane(v0, v1, v2, start, bufA[0], bufA[1], bufA[2], bufA[3]);
+        if (!nv) {
+            ClipPos bufB[kClipMax];
+            bufA[0] = v0;
+            bufA[1] = v1;
+            bufA[2] = v2;
+            nv = clip_triangle(bufA, bufB, start);
+        }
+    }
+    uint32_t produced = 0;
+    if (nv >= 3) {
+        for (int j = 0; j < nv; j++) persp_divide(bufA[j]);
+        for (int j = 1; j + 1 < nv; j++) {
+            TriBox tb;
+            produced += tri_box(R.rs, dims, bufA[0].clip, bufA[j].clip, bufA[j + 1].clip, tb) == kTriFill ? 1u : 0u;
+        }
+    }
+    return produced;
+}
+
 // The listed triangles: Sutherland-Hodgman from the first plane that is not all-inside, then
 // the fan. Grid-strided over the list (its length is on the device), with the grid capped
 // so that the resident threads' clip buffers fit in cache.
@@ -1096,29 +1199,18 @@ __global__ void __launch_bounds__(64) k_clip(GeomArgs A)
         const RecOut o = rec_out(A, t, EMIT, EYE);
         uint32_t e0, e1, e2;
         element_triple(D.mode, P.k, e0, e1, e2);
-        V v0, v1, v2;
-        load_cv(A, element_slot(D, e0), v0);
-        load_cv(A, element_slot(D, e1), v1);
-        load_cv(A, element_slot(D, e2), v2);
-        const int start = clip_start(inside_mask(v0.clip), inside_mask(v1.clip), inside_mask(v2.clip));
-        uint32_t produced = 0;
-        V bufA[kClipMax];
-        int nv = 0;
-        if (start < kClipNone) {
-            // one plane crossed: the pass in registers; otherwise the general clipper
-            nv = clip_one_plane(v0, v1, v2, start, bufA[0], bufA[1], bufA[2], bufA[3]);
-            if (!nv) {
-                V bufB[kClipMax];
-                bufA[0] = v0;
-                bufA[1] = v1;
-                bufA[2] = v2;
-                nv = clip_triangle(bufA, bufB, start);
-            }
-        }
-        if (nv >= 3) {
-            for (int j = 0; j < nv; j++) persp_divide(bufA[j]);
-            for (int j = 1; j + 1 < nv; j++)
-                produced += setup_fan_tri(R, D.raster, P.frame, P.dims, bufA[0], bufA[j], bufA[j + 1], o, produced);
+        const uint32_t s0 = element_slot(D, e0), s1 = element_slot(D, e1), s2 = element_slot(D, e2);
+        uint32_t produced;
+        if (!EMIT && R.rs.polygon_mode_front == GL_FILL && R.rs.polygon_mode_back == GL_FILL) {
+            // counting a filled triangle: clip the positions alone
+            produced = clip_fan_count(R, P.dims, ClipPos{A.verts.clip[s0]}, ClipPos{A.verts.clip[s1]},
+                                      ClipPos{A.verts.clip[s2]});
+        } else {
+            V v0, v1, v2;
+            load_cv(A, s0, v0);
+            load_cv(A, s1, v1);
+            load_cv(A, s2, v2);
+            produced = clip_fan(R, D.raster, P.frame, P.dims, v0, v1, v2, o);
         }
         if (!EMIT) A.tri_counts[t] = produced;
     }

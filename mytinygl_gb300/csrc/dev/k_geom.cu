@@ -1050,21 +1050,39 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
         } else {
             uint32_t e0, e1, e2;
             element_triple(D.mode, P.k, e0, e1, e2);
-            V v0, v1, v2;
-            load_cv(A, element_slot(D, e0), v0);
-            load_cv(A, element_slot(D, e1), v1);
-            load_cv(A, element_slot(D, e2), v2);
-            const uint32_t m0 = inside_mask(v0.clip), m1 = inside_mask(v1.clip), m2 = inside_mask(v2.clip);
-            const int start = clip_start(m0, m1, m2);
-            if (start == kClipNone) {  // the clipper would return the triangle unchanged
-                persp_divide(v0);
-                persp_divide(v1);
-                persp_divide(v2);
-                produced = setup_fan_tri(R, D.raster, P.frame, P.dims, v0, v1, v2, o, 0);
-            } else if (start != kClipEmpty) {
-                if (EMIT) return;  // k_clip emits it
-                cls = A.clip_sorted ? clip_class(m0, m1, m2, start) : 0u;
-                straddles = true;
+            const uint32_t s0 = element_slot(D, e0), s1 = element_slot(D, e1), s2 = element_slot(D, e2);
+            if (!EMIT && R.rs.polygon_mode_front == GL_FILL && R.rs.polygon_mode_back == GL_FILL) {
+                // counting a filled triangle: its positions decide (the clip's count pass, the same)
+                ClipPos v0{A.verts.clip[s0]}, v1{A.verts.clip[s1]}, v2{A.verts.clip[s2]};
+                const uint32_t m0 = inside_mask(v0.clip), m1 = inside_mask(v1.clip), m2 = inside_mask(v2.clip);
+                const int start = clip_start(m0, m1, m2);
+                if (start == kClipNone) {
+                    persp_divide(v0);
+                    persp_divide(v1);
+                    persp_divide(v2);
+                    TriBox tb;
+                    produced = tri_box(R.rs, P.dims, v0.clip, v1.clip, v2.clip, tb) == kTriFill ? 1u : 0u;
+                } else if (start != kClipEmpty) {
+                    cls = A.clip_sorted ? clip_class(m0, m1, m2, start) : 0u;
+                    straddles = true;
+                }
+            } else {
+                V v0, v1, v2;
+                load_cv(A, s0, v0);
+                load_cv(A, s1, v1);
+                load_cv(A, s2, v2);
+                const uint32_t m0 = inside_mask(v0.clip), m1 = inside_mask(v1.clip), m2 = inside_mask(v2.clip);
+                const int start = clip_start(m0, m1, m2);
+                if (start == kClipNone) {  // the clipper would return the triangle unchanged
+                    persp_divide(v0);
+                    persp_divide(v1);
+                    persp_divide(v2);
+                    produced = setup_fan_tri(R, D.raster, P.frame, P.dims, v0, v1, v2, o, 0);
+                } else if (start != kClipEmpty) {
+                    if (EMIT) return;  // k_clip emits it
+                    cls = A.clip_sorted ? clip_class(m0, m1, m2, start) : 0u;
+                    straddles = true;
+                }
             }
         }
     }

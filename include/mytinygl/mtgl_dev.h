@@ -153,7 +153,9 @@ typedef struct {
     uint64_t vertices;             /* vertex slots transformed by the vertex stage */
     uint64_t vertex_bytes;         /* attribute bytes those slots read (enabled arrays) */
     uint64_t debug_status;         /* build with MTGL_DEBUG_BOUNDS: the site code of the first
-                                      device index check that failed (0: none); else 0 */
+                                      device index check that failed (0: none). Any build: 7
+                                      when a scan's bounded wait for an earlier block ran out
+                                      (never expected; the pass's results are then wrong) */
 } mtgl_stats;
 
 /* Device time per pipeline phase, summed over the passes since profiling was enabled

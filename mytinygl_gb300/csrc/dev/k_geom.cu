@@ -1052,7 +1052,7 @@ __global__ void __launch_bounds__(128) k_setup(GeomArgs A)
             element_triple(D.mode, P.k, e0, e1, e2);
             const uint32_t s0 = element_slot(D, e0), s1 = element_slot(D, e1), s2 = element_slot(D, e2);
             if (!EMIT && R.rs.polygon_mode_front == GL_FILL && R.rs.polygon_mode_back == GL_FILL) {
-                // counting a filled triangle: its positions decide (the clip's count pass, the same)
+                // counting a filled triangle: its positions alone decide (as in k_clip's count pass)
                 ClipPos v0{A.verts.clip[s0]}, v1{A.verts.clip[s1]}, v2{A.verts.clip[s2]};
                 const uint32_t m0 = inside_mask(v0.clip), m1 = inside_mask(v1.clip), m2 = inside_mask(v2.clip);
                 const int start = clip_start(m0, m1, m2);

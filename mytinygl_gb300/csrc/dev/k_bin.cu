@@ -258,7 +258,7 @@ __device__ __forceinline__ bool tile_gets_pair(const RecTiles &t, int i)
     return ok;
 }
 
-constexpr uint32_t kCountLanes = 4;  // lanes per record in k_bin_count (8 records per warp)
+constexpr uint32_t kCountLanes = 2;  // lanes per record in k_bin_count (16 records per warp)
 
 // pairs per record; records past the real count get 0 so the scan over the capacity is exact
 __global__ void __launch_bounds__(256) k_bin_count(BinArgs A)

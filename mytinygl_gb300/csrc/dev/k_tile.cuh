@@ -12,9 +12,9 @@
 // in-order blending and stencil updates need no atomics. Clears of the pass are applied
 // first; a clear that covers the whole tile means that buffer is never read from memory.
 //
-// The launch is persistent: CTAs take tiles from a work queue (an atomic head over a list
-// of global tile ids, costliest first in batches) until it is empty, so frames of very
-// different sizes share one launch without idle SMs at its end.
+// The launch is persistent: CTAs take tiles from a work queue (an atomic head over the
+// global tile ids, in frame order or, when the pass asks for it, costliest first) until it
+// is empty, so frames of very different sizes share one launch without idle SMs at its end.
 #pragma once
 
 #include <algorithm>

@@ -6,7 +6,7 @@
 // blocks) and runs the pipeline once: K1 over all vertices, K2 over all triangles, K3 over
 // the tiles of all frames, and a persistent K4 whose CTAs drain a device queue of
 // (frame, tile) items (in frame order by default, or costliest first: the batch config's
-// order). The run has no host waits (record and pair
+// order_by_cost). The run has no host waits (record and pair
 // buffers have fixed capacities, checked on the device), so it is captured once as a CUDA
 // graph and replayed for as long as the batch's shape (tables, capacities, buffers) stays
 // the same; only the staged bytes change between replays.

@@ -462,7 +462,7 @@ int run_pipeline(Exec &x, ScratchSource &sc, const HostStage &st, const Tables &
     if (eye && (rc = sc.take(S_EYES, slots, &eyes))) return rc;
     if ((rc = sc.take(S_TRI_COUNTS, tris, &tri_counts))) return rc;
     if ((rc = sc.take(S_TRI_OFFSETS, tris, &tri_offsets))) return rc;
-    // clip list, its class words, the class-sorted list and the class counters
+    // clip list, its class words, the class-sorted list, the class counters and the emit list
     uint32_t *clip_list = nullptr;
     if ((rc = sc.take(S_CLIP_LIST, 4 * (size_t)tris + kClipBuckets, &clip_list))) return rc;
     // tile counts, then (persistent ordered launches) the per-tile record-box coverage
